@@ -1,0 +1,99 @@
+/*
+ * sister_gb300 -- GB300 (sm_103a) implementation of SiSter's 5-view multiview disparity.
+ *
+ * C ABI of libsister_gb300.so. Plain pointers and sizes only. Every entry point returns a status
+ * (SISTER_OK = 0 or a negative SISTER_E* code); sister_last_error() gives the message.
+ *
+ * Reference interface replaced (paths relative to the reference project root):
+ *   class SisterMultiviewDisparities                     cpp/include/sister/SisterMultiviewDisparities.hpp:18
+ *     ctor (center, right, top, left, bottom)            ...SisterMultiviewDisparities.hpp:22
+ *     compute_disparities(dispCount, multi, horiz, vert) ...SisterMultiviewDisparities.hpp:26-119
+ *   callers: cpp/src/compute_disp.cpp:26-35 and the ROS service recipe ros/README.md:47-56.
+ *
+ * Outputs follow the reference exactly: u16 images of the ORIGINAL size w x h holding disparity*255
+ * (saturated at 65535), bit-exact with the reference CPU path on the same input. Inputs are 8-bit
+ * images, either gray (channels = 1) or BGR (channels = 3, converted with OpenCV's published
+ * fixed-point BGR2GRAY weights). Preconditions the reference leaves implicit are checked:
+ * w % 4 == 0, h % 4 == 0, 8 <= dc <= 512, dc % 8 == 0.
+ */
+#ifndef SISTER_GB300_H
+#define SISTER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SISTER_API __attribute__((visibility("default")))
+#else
+#define SISTER_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SISTER_OK = 0,
+    SISTER_EINVAL = -1,   /* bad argument / unsupported geometry */
+    SISTER_ENOMEM = -2,   /* device allocation failed */
+    SISTER_EBUDGET = -3,  /* request exceeds the configured HBM budget (serving) */
+    SISTER_EDEVICE = -4,  /* CUDA error */
+    SISTER_ETIMEOUT = -5, /* a bounded device-side wait expired */
+    SISTER_ESTATE = -6    /* call order violated (e.g. compute before load) */
+};
+
+typedef struct sister_ctx sister_ctx;
+
+/* --- plain drop-in path (one rig at a time) -------------------------------------------------- */
+
+/* Create a context on CUDA device `device`. Replaces constructing SisterMultiviewDisparities. */
+SISTER_API int sister_ctx_create(sister_ctx **out, int device);
+SISTER_API void sister_ctx_destroy(sister_ctx *ctx);
+SISTER_API const char *sister_last_error(const sister_ctx *ctx);
+
+/* Load the five views in the reference constructor's order {center, right, top, left, bottom}
+ * (SisterMultiviewDisparities.hpp:22), each `height` rows of `width` pixels with row pitch `stride`
+ * bytes, `channels` 1 (gray) or 3 (BGR, SisterMultiviewDisparities.hpp:29-33). Host pointers. */
+SISTER_API int sister_load_views(sister_ctx *ctx, const uint8_t *const views[5], int width, int height, int stride,
+                      int channels);
+/* Same, with device pointers (images already resident in HBM). */
+SISTER_API int sister_load_views_device(sister_ctx *ctx, const uint8_t *const views[5], int width, int height,
+                             int stride, int channels);
+
+/* The dispCount argument of compute_disparities (SisterMultiviewDisparities.hpp:26). */
+SISTER_API int sister_set_max_disparity(sister_ctx *ctx, int dc);
+
+/* compute_disparities (SisterMultiviewDisparities.hpp:26-119): writes width*height u16 images to host
+ * buffers. `multi` is mode 0 (all four pairs), `horiz` mode 1, `vert` mode 2; any may be NULL and the
+ * corresponding aggregation is then skipped. Blocks until the results are on the host. */
+SISTER_API int sister_compute(sister_ctx *ctx, uint16_t *multi, uint16_t *horiz, uint16_t *vert);
+/* Same with device output pointers; asynchronous on the context stream (see sister_synchronize). */
+SISTER_API int sister_compute_device(sister_ctx *ctx, uint16_t *multi, uint16_t *horiz, uint16_t *vert);
+
+/* Use an external cudaStream_t (NULL restores the context's own stream). */
+SISTER_API int sister_set_stream(sister_ctx *ctx, void *stream);
+/* Wait for queued work; reports device-side errors (e.g. SISTER_ETIMEOUT) of completed launches. */
+SISTER_API int sister_synchronize(sister_ctx *ctx);
+
+/* Bytes of device memory the context would hold for a w x h rig at max disparity dc
+ * (one mode; add the aggregation volume once more per extra mode computed concurrently). */
+SISTER_API size_t sister_device_bytes(int width, int height, int dc);
+
+/* --- test hooks: intermediates of the last compute (device -> host copies) -------------------- */
+enum {
+    SISTER_DBG_FRAMES = 1, /* index k=0..7: frame image k (u8) */
+    SISTER_DBG_CENSUS = 2, /* index k=0..7: census of frame image k (u64) */
+    SISTER_DBG_WTA = 3,    /* index 2f / 2f+1: WTA-left / WTA-right of frame f before the median (u16) */
+    SISTER_DBG_MEDIAN = 4, /* index 2f / 2f+1: after the in-place median (u16) */
+    SISTER_DBG_MASKS = 5,  /* index f: confidence mask of frame f in padded original coordinates (u8) */
+    SISTER_DBG_COST = 6,   /* index 0: masked multiview cost of the last aggregated mode (u16, d stride dp) */
+    SISTER_DBG_SUM0 = 7,   /* index 0: pass-0 SGM sum of the last aggregated mode (u16, d stride dp) */
+    SISTER_DBG_DISP = 8,   /* index mode: padded winner-take-all disparity (u16, Hp x Wp) */
+    SISTER_DBG_DP = 9      /* returns the padded disparity stride dp of the volumes in *(int*)dst */
+};
+SISTER_API int sister_debug_fetch(sister_ctx *ctx, int what, int index, void *host_dst, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

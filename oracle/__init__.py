@@ -122,12 +122,23 @@ class Port(_Lib):
         self.lib.orc_lrc_mask(_ptr(L, _u16p), _ptr(R, _u16p), W, H, dc, _ptr(m, _u8p))
         return m
 
-    def sgm(self, C):
+    def sgm(self, C, npasses: int = 2):
         C = np.ascontiguousarray(C, np.uint16)
         H, W, D = C.shape
         S = np.zeros_like(C)
-        self.lib.orc_sgm(_ptr(C, _u16p), W, H, D, _ptr(S, _u16p))
+        self.lib.orc_sgm_passes(_ptr(C, _u16p), W, H, D, _ptr(S, _u16p), int(npasses))
         return S
+
+    def masked_cost(self, census, masks, dc, mode):
+        """census: 8 frame census images (u64), masks: 4 x Hp x Wp (u8) -> M (Hp x Wp x dc u16)."""
+        cs = [np.ascontiguousarray(c, np.uint64) for c in census]
+        ms = [np.ascontiguousarray(m, np.uint8) for m in masks]
+        Hp, Wp = ms[0].shape
+        carr = (_u64p * 8)(*[_ptr(c, _u64p) for c in cs])
+        marr = (_u8p * 4)(*[_ptr(m, _u8p) for m in ms])
+        M = np.zeros((Hp, Wp, dc), np.uint16)
+        self.lib.orc_masked_cost(carr, marr, Wp, Hp, dc, int(mode), _ptr(M, _u16p))
+        return M
 
     def wta_left_vol(self, vol):
         vol = np.ascontiguousarray(vol, np.uint16)

@@ -256,7 +256,7 @@ void orc_masked_cost(const uint64_t *const census[8], const uint8_t *const masks
  *    L_r(d) = C(d) +s ( min(Lp(d), Lp(d-1) +s 7, Lp(d+1) +s 7, minLp +s 100) -s minLp ) with u16
  *    saturating +s/-s; r0 restarts each row from Lp = 0, minLp = 0 (:215-216). The sum is
  *    ((r0 +s r1) +s r2) +s r3, stored in pass 0 and added saturating in pass 1 (:386-391). */
-void orc_sgm(const uint16_t *C, int W, int H, int D, uint16_t *S) {
+void orc_sgm_passes(const uint16_t *C, int W, int H, int D, uint16_t *S, int npasses) {
     const int P = D + 2;
     const size_t colsz = (size_t)(W + 2) * P;
     uint16_t *r1last = (uint16_t *)malloc(colsz * 2), *r1cur = (uint16_t *)malloc(colsz * 2);
@@ -271,7 +271,7 @@ void orc_sgm(const uint16_t *C, int W, int H, int D, uint16_t *S) {
     for (int k = 0; k < P; k++) r0prev[k] = r0new[k] = t2[k] = t3[k] = INF16;
 
 #define ST(arr, c, d) (arr)[(size_t)((c) + 1) * P + (d) + 1]
-    for (int pass = 0; pass < 2; pass++) {
+    for (int pass = 0; pass < npasses; pass++) {
         const int di = pass ? -1 : 1, dj = di;
         const int i1 = pass ? H - 1 : 0, j1 = pass ? W - 1 : 0;
         const int iend = pass ? -1 : H, jend = pass ? -1 : W;
@@ -374,6 +374,8 @@ out:
     free(m1last); free(m1cur); free(m2); free(m3);
     free(r0prev); free(r0new); free(t2); free(t3);
 }
+
+void orc_sgm(const uint16_t *C, int W, int H, int D, uint16_t *S) { orc_sgm_passes(C, W, H, D, S, 2); }
 
 /* Final WTALeft_SSE(outputL, sum_dsi, Wp, Hp, dc-1, 1) (hpp:283): first argmin over d <= min(j, D-1). */
 void orc_wta_left_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp) {

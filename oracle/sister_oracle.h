@@ -57,6 +57,8 @@ void orc_masked_cost(const uint64_t *const census[8], const uint8_t *const masks
 
 /* 8-path SGM, P1=7, P2=100, two passes with the reference's first-line semantics (sgm.cpp:26-455). */
 void orc_sgm(const uint16_t *C, int W, int H, int D, uint16_t *S);
+/* The same, stopping after `npasses` (1: pass 0 only, leaving the pass-0 sum in S). */
+void orc_sgm_passes(const uint16_t *C, int W, int H, int D, uint16_t *S, int npasses);
 
 /* WTA-left (argmin over d<=min(j,D-1), lowest d on ties) of a volume. */
 void orc_wta_left_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp);

@@ -1,0 +1,169 @@
+"""sister_gb300: SiSter's 5-view multiview disparity on GB300 (sm_103a), bit-exact with the reference.
+
+Python mirror of the reference helper class (cpp/include/sister/SisterMultiviewDisparities.hpp:18-119)
+over the C ABI of libsister_gb300.so (include/sister_gb300.h):
+
+    m = SisterMultiviewDisparities(center, right, top, left, bottom)   # hpp:22
+    multi, horiz, vert = m.compute_disparities(dispCount)               # hpp:26
+
+Inputs are u8 images (h x w gray, or h x w x 3 BGR); outputs are u16 h x w images holding disparity*255.
+There is no CPU fallback: if the CUDA library is missing or no GPU is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["SisterMultiviewDisparities", "Context", "SisterError", "load_library", "LIB_PATH"]
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_gb300.so")
+
+SISTER_OK = 0
+_ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
+
+DBG_FRAMES, DBG_CENSUS, DBG_WTA, DBG_MEDIAN, DBG_MASKS, DBG_COST, DBG_SUM0, DBG_DISP, DBG_DP = range(1, 10)
+
+
+class SisterError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "E?"), code, msg))
+        self.code = code
+
+
+_lib = None
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u16p = ctypes.POINTER(ctypes.c_uint16)
+_vp = ctypes.c_void_p
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load libsister_gb300.so (build it with `python -m sister_gb300.build`). Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError("libsister_gb300.so not built (%s); run `python -m sister_gb300.build`" % p)
+    lib = ctypes.CDLL(p)
+    lib.sister_ctx_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
+    lib.sister_ctx_destroy.argtypes = [_vp]
+    lib.sister_ctx_destroy.restype = None
+    lib.sister_last_error.argtypes = [_vp]
+    lib.sister_last_error.restype = ctypes.c_char_p
+    lib.sister_load_views.argtypes = [_vp, ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.sister_load_views_device.argtypes = lib.sister_load_views.argtypes
+    lib.sister_set_max_disparity.argtypes = [_vp, ctypes.c_int]
+    lib.sister_compute.argtypes = [_vp, _vp, _vp, _vp]
+    lib.sister_compute_device.argtypes = [_vp, _vp, _vp, _vp]
+    lib.sister_set_stream.argtypes = [_vp, _vp]
+    lib.sister_synchronize.argtypes = [_vp]
+    lib.sister_device_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.sister_device_bytes.restype = ctypes.c_size_t
+    lib.sister_debug_fetch.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_size_t]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _as_views(views):
+    out = []
+    for v in views:
+        a = np.ascontiguousarray(v, dtype=np.uint8)
+        if a.ndim not in (2, 3) or (a.ndim == 3 and a.shape[2] != 3):
+            raise ValueError("views must be h x w (gray) or h x w x 3 (BGR) uint8 arrays")
+        out.append(a)
+    shapes = {a.shape for a in out}
+    if len(shapes) != 1:
+        raise ValueError("all five views must have the same shape, got %s" % sorted(shapes))
+    return out
+
+
+class Context:
+    """One device context (sister_ctx): owns device buffers and a stream; not thread-safe."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.sister_ctx_create(ctypes.byref(h), int(device))
+        if rc != SISTER_OK:
+            raise SisterError(rc, "sister_ctx_create(device=%d) failed" % device)
+        self.h = h
+        self.shape = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sister_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != SISTER_OK:
+            raise SisterError(rc, self.lib.sister_last_error(self.h).decode(errors="replace"))
+
+    def load_views(self, views):
+        vs = _as_views(views)
+        h, w = vs[0].shape[:2]
+        ch = 3 if vs[0].ndim == 3 else 1
+        arr = (ctypes.c_void_p * 5)(*[v.ctypes.data for v in vs])
+        self._check(self.lib.sister_load_views(self.h, arr, w, h, w * ch, ch))
+        self.shape = (h, w)
+        self._keep = vs
+
+    def load_views_device(self, ptrs, width: int, height: int, stride: int, channels: int = 1):
+        arr = (ctypes.c_void_p * 5)(*[int(p) for p in ptrs])
+        self._check(self.lib.sister_load_views_device(self.h, arr, width, height, stride, channels))
+        self.shape = (height, width)
+
+    def set_max_disparity(self, dc: int):
+        self._check(self.lib.sister_set_max_disparity(self.h, int(dc)))
+
+    def compute(self, multi=True, horiz=False, vert=False):
+        h, w = self.shape
+        outs = [np.empty((h, w), np.uint16) if f else None for f in (multi, horiz, vert)]
+        ptrs = [o.ctypes.data if o is not None else None for o in outs]
+        self._check(self.lib.sister_compute(self.h, *ptrs))
+        return outs
+
+    def compute_device(self, multi_ptr=None, horiz_ptr=None, vert_ptr=None):
+        self._check(self.lib.sister_compute_device(self.h, multi_ptr, horiz_ptr, vert_ptr))
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.sister_set_stream(self.h, stream_ptr))
+
+    def synchronize(self):
+        self._check(self.lib.sister_synchronize(self.h))
+
+    def debug(self, what: int, index: int, shape, dtype):
+        out = np.empty(shape, dtype)
+        self._check(self.lib.sister_debug_fetch(self.h, what, index, out.ctypes.data, out.nbytes))
+        return out
+
+    def debug_dp(self) -> int:
+        v = ctypes.c_int(0)
+        self._check(self.lib.sister_debug_fetch(self.h, DBG_DP, 0, ctypes.addressof(v), 4))
+        return v.value
+
+
+class SisterMultiviewDisparities:
+    """Drop-in for the reference helper class (SisterMultiviewDisparities.hpp:18-119).
+
+    Views are given in the reference constructor order: center, right, top, left, bottom.
+    compute_disparities(dispCount) returns (disp_multiview, disp_horizontal, disp_vertical), u16 h x w
+    images of disparity*255, exactly as the reference's output Mats.
+    """
+
+    def __init__(self, center, right, top, left, bottom, device: int = 0):
+        self.views = _as_views([center, right, top, left, bottom])
+        self.ctx = Context(device)
+        self.ctx.load_views(self.views)
+
+    def compute_disparities(self, dispCount: int, multiview=True, horizontal=True, vertical=True):
+        self.ctx.set_max_disparity(dispCount)
+        return tuple(self.ctx.compute(multiview, horizontal, vertical))

@@ -1,0 +1,389 @@
+// Host runtime of libsister_gb300: context, device buffers, stage orchestration and the C ABI of
+// include/sister_gb300.h.
+#include "sister_gb300.h"
+#include "sister_internal.h"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace sister;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return e;
+        }
+        cap = bytes;
+        return cudaSuccess;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+std::mutex g_init_mu;
+std::vector<int> g_inited_devices;
+
+void init_device_kernels(int dev) {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    for (int d : g_inited_devices)
+        if (d == dev) return;
+    init_mask_kernels();
+    init_sgm_kernels();
+    g_inited_devices.push_back(dev);
+}
+
+} // namespace
+
+struct sister_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool loaded = false;
+    int w = 0, h = 0, dc = 0;
+    DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, bnd, bmin, progress, errflag, disp, outs;
+    int last_mode = -1;
+    bool have_intermediates = false;
+    Geom g{};
+
+    int fail(int code, const char *fmt, ...) __attribute__((format(printf, 3, 4))) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what) {
+        cudaGetLastError();
+        if (e == cudaErrorMemoryAllocation) return fail(SISTER_ENOMEM, "%s: %s", what, cudaGetErrorString(e));
+        return fail(SISTER_EDEVICE, "%s: %s", what, cudaGetErrorString(e));
+    }
+};
+
+namespace {
+
+int check_geometry(sister_ctx *c, int w, int h, int dc) {
+    if (w < 4 || h < 4 || (w % 4) || (h % 4))
+        return c->fail(SISTER_EINVAL, "image size %dx%d: width and height must be positive multiples of 4", w, h);
+    if (dc < 8 || dc > 512 || (dc % 8))
+        return c->fail(SISTER_EINVAL, "max disparity %d: must be a multiple of 8 in [8, 512]", dc);
+    return SISTER_OK;
+}
+
+int load_common(sister_ctx *c, const uint8_t *const views[5], int width, int height, int stride, int channels,
+                bool device_ptrs) {
+    if (!views) return c->fail(SISTER_EINVAL, "views is NULL");
+    for (int k = 0; k < 5; k++)
+        if (!views[k]) return c->fail(SISTER_EINVAL, "view %d is NULL", k);
+    if (channels != 1 && channels != 3) return c->fail(SISTER_EINVAL, "channels must be 1 or 3, got %d", channels);
+    if (width < 4 || height < 4 || (width % 4) || (height % 4))
+        return c->fail(SISTER_EINVAL, "image size %dx%d: width and height must be positive multiples of 4", width,
+                       height);
+    if (stride < width * channels) return c->fail(SISTER_EINVAL, "stride %d < width*channels", stride);
+    cudaSetDevice(c->device);
+    const size_t plane = (size_t)width * height;
+    cudaError_t e = c->views.ensure(5 * plane);
+    if (e != cudaSuccess) return c->cuda_fail(e, "allocating views");
+    const uint8_t *src[5];
+    if (device_ptrs) {
+        for (int k = 0; k < 5; k++) src[k] = views[k];
+        launch_to_gray(src, stride, channels, width, height, c->views.as<uint8_t>(), c->stream);
+    } else {
+        const size_t row = (size_t)width * channels;
+        if (channels == 1) {
+            for (int k = 0; k < 5; k++) {
+                e = cudaMemcpy2DAsync(c->views.as<uint8_t>() + k * plane, width, views[k], stride, width, height,
+                                      cudaMemcpyHostToDevice, c->stream);
+                if (e != cudaSuccess) return c->cuda_fail(e, "copying views");
+            }
+        } else {
+            e = c->raw.ensure(5 * row * height);
+            if (e != cudaSuccess) return c->cuda_fail(e, "allocating raw views");
+            for (int k = 0; k < 5; k++) {
+                e = cudaMemcpy2DAsync(c->raw.as<uint8_t>() + k * row * height, row, views[k], stride, row, height,
+                                      cudaMemcpyHostToDevice, c->stream);
+                if (e != cudaSuccess) return c->cuda_fail(e, "copying views");
+                src[k] = c->raw.as<uint8_t>() + k * row * height;
+            }
+            launch_to_gray(src, (int)row, 3, width, height, c->views.as<uint8_t>(), c->stream);
+        }
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return c->cuda_fail(e, "loading views");
+    c->w = width;
+    c->h = height;
+    c->loaded = true;
+    c->have_intermediates = false;
+    return SISTER_OK;
+}
+
+int ensure_buffers(sister_ctx *c, const Geom &g) {
+    const size_t plane = g.plane, vol = plane * g.dp;
+    const int R = sgm_rows_per_band(g, c->num_sms);
+    const size_t nb = (size_t)(g.Hp + R - 1) / R;
+    struct {
+        DevBuf *b;
+        size_t bytes;
+        const char *what;
+    } req[] = {
+        {&c->frames, 8 * plane, "frames"},
+        {&c->census, 8 * plane * sizeof(uint64_t), "census"},
+        {&c->wta, 8 * plane * sizeof(uint16_t), "wta"},
+        {&c->med, 8 * plane * sizeof(uint16_t), "median"},
+        {&c->masks, 4 * plane, "masks"},
+        {&c->cost, vol * sizeof(uint16_t), "cost volume"},
+        {&c->sum0, vol * sizeof(uint16_t), "sum volume"},
+        {&c->bnd, sgm_bnd_elems(g, c->num_sms) * sizeof(uint16_t), "band states"},
+        {&c->bmin, nb * g.Wp * 4 * sizeof(uint16_t), "band minima"},
+        {&c->progress, nb * sizeof(unsigned), "progress"},
+        {&c->errflag, sizeof(unsigned), "error flag"},
+        {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
+        {&c->outs, 3 * (size_t)g.w * g.h * sizeof(uint16_t), "outputs"},
+    };
+    for (auto &r : req) {
+        cudaError_t e = r.b->ensure(r.bytes);
+        if (e != cudaSuccess) return c->cuda_fail(e, r.what);
+    }
+    return SISTER_OK;
+}
+
+// The whole compute_disparities pipeline on the context stream; outputs (device) may be null.
+int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
+    if (!c->loaded) return c->fail(SISTER_ESTATE, "no views loaded");
+    if (!c->dc) return c->fail(SISTER_ESTATE, "max disparity not set");
+    int rc = check_geometry(c, c->w, c->h, c->dc);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    const Geom g = make_geom(c->w, c->h, c->dc);
+    rc = ensure_buffers(c, g);
+    if (rc) return rc;
+    c->g = g;
+    cudaStream_t st = c->stream;
+    cudaError_t e = cudaMemsetAsync(c->errflag.p, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "reset error flag");
+    launch_frames(c->views.as<uint8_t>(), g, c->frames.as<uint8_t>(), st);
+    launch_census(c->frames.as<uint8_t>(), g, c->census.as<uint64_t>(), st);
+    launch_pair_wta(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), st);
+    launch_median(c->wta.as<uint16_t>(), g, c->med.as<uint16_t>(), st);
+    launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
+    const int R = sgm_rows_per_band(g, c->num_sms);
+    for (int mode = 0; mode < 3; mode++) {
+        if (!dev_out[mode]) continue;
+        launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
+        SgmArgs a{};
+        a.cost = c->cost.as<uint16_t>();
+        a.sum0 = c->sum0.as<uint16_t>();
+        a.bnd = c->bnd.as<uint16_t>();
+        a.bmin = c->bmin.as<uint16_t>();
+        a.progress = c->progress.as<unsigned>();
+        a.err = c->errflag.as<unsigned>();
+        a.out = dev_out[mode];
+        a.disp = c->disp.as<uint16_t>() + (size_t)mode * g.plane;
+        a.W = g.Wp;
+        a.H = g.Hp;
+        a.D = g.dc;
+        a.dp = g.dp;
+        a.dc = g.dc;
+        a.w = g.w;
+        a.h = g.h;
+        a.R = R;
+        a.nbands = (g.Hp + R - 1) / R;
+        a.spin_limit = 1u << 22;
+        e = launch_sgm(g, a, st, c->device);
+        if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
+        c->last_mode = mode;
+    }
+    c->have_intermediates = true;
+    return SISTER_OK;
+}
+
+int read_device_error(sister_ctx *c) {
+    unsigned flag = 0;
+    cudaError_t e = cudaMemcpy(&flag, c->errflag.p, sizeof flag, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return c->cuda_fail(e, "reading device error flag");
+    if (flag == kErrTimeout)
+        return c->fail(SISTER_ETIMEOUT, "aggregation band hand-off wait expired (device reported timeout)");
+    return SISTER_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int sister_ctx_create(sister_ctx **out, int device) {
+    if (!out) return SISTER_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return SISTER_EDEVICE;
+    }
+    sister_ctx *c = new (std::nothrow) sister_ctx();
+    if (!c) return SISTER_ENOMEM;
+    c->device = device;
+    cudaSetDevice(device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    if (!coop || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return SISTER_EDEVICE;
+    }
+    c->stream = c->own_stream;
+    init_device_kernels(device);
+    if (c->errflag.ensure(sizeof(unsigned)) != cudaSuccess) {
+        delete c;
+        return SISTER_ENOMEM;
+    }
+    *out = c;
+    return SISTER_OK;
+}
+
+void sister_ctx_destroy(sister_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->own_stream) {
+        cudaStreamSynchronize(c->own_stream);
+        cudaStreamDestroy(c->own_stream);
+    }
+    delete c;
+}
+
+const char *sister_last_error(const sister_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int sister_load_views(sister_ctx *c, const uint8_t *const views[5], int width, int height, int stride,
+                      int channels) {
+    if (!c) return SISTER_EINVAL;
+    return load_common(c, views, width, height, stride, channels, false);
+}
+
+int sister_load_views_device(sister_ctx *c, const uint8_t *const views[5], int width, int height, int stride,
+                             int channels) {
+    if (!c) return SISTER_EINVAL;
+    return load_common(c, views, width, height, stride, channels, true);
+}
+
+int sister_set_max_disparity(sister_ctx *c, int dc) {
+    if (!c) return SISTER_EINVAL;
+    if (dc < 8 || dc > 512 || (dc % 8))
+        return c->fail(SISTER_EINVAL, "max disparity %d: must be a multiple of 8 in [8, 512]", dc);
+    c->dc = dc;
+    return SISTER_OK;
+}
+
+int sister_compute_device(sister_ctx *c, uint16_t *multi, uint16_t *horiz, uint16_t *vert) {
+    if (!c) return SISTER_EINVAL;
+    uint16_t *o[3] = {multi, horiz, vert};
+    return run_pipeline(c, o);
+}
+
+int sister_compute(sister_ctx *c, uint16_t *multi, uint16_t *horiz, uint16_t *vert) {
+    if (!c) return SISTER_EINVAL;
+    if (!c->loaded) return c->fail(SISTER_ESTATE, "no views loaded");
+    if (!c->dc) return c->fail(SISTER_ESTATE, "max disparity not set");
+    int rc = check_geometry(c, c->w, c->h, c->dc);
+    if (rc) return rc;
+    cudaSetDevice(c->device);
+    rc = ensure_buffers(c, make_geom(c->w, c->h, c->dc));
+    if (rc) return rc;
+    const size_t n = (size_t)c->w * c->h;
+    uint16_t *host[3] = {multi, horiz, vert};
+    uint16_t *dev[3];
+    for (int m = 0; m < 3; m++) dev[m] = host[m] ? c->outs.as<uint16_t>() + (size_t)m * n : nullptr;
+    rc = run_pipeline(c, dev);
+    if (rc) return rc;
+    for (int m = 0; m < 3; m++) {
+        if (!host[m]) continue;
+        cudaError_t e = cudaMemcpyAsync(host[m], dev[m], n * sizeof(uint16_t), cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return c->cuda_fail(e, "copying result");
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "compute");
+    return read_device_error(c);
+}
+
+int sister_set_stream(sister_ctx *c, void *stream) {
+    if (!c) return SISTER_EINVAL;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return SISTER_OK;
+}
+
+int sister_synchronize(sister_ctx *c) {
+    if (!c) return SISTER_EINVAL;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "synchronize");
+    return read_device_error(c);
+}
+
+size_t sister_device_bytes(int width, int height, int dc) {
+    if (width <= 0 || height <= 0 || dc <= 0) return 0;
+    const Geom g = make_geom(width, height, dc);
+    if (g.dpl < 0) return 0;
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    const size_t plane = g.plane, vol = plane * g.dp;
+    const int R = sgm_rows_per_band(g, sms);
+    const size_t nb = (size_t)(g.Hp + R - 1) / R;
+    return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 2 * vol * 2 +
+           sgm_bnd_elems(g, sms) * 2 + nb * g.Wp * 8 + nb * 4 + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+}
+
+int sister_debug_fetch(sister_ctx *c, int what, int index, void *dst, size_t bytes) {
+    if (!c || !dst) return SISTER_EINVAL;
+    if (what == SISTER_DBG_DP) {
+        if (bytes < sizeof(int)) return SISTER_EINVAL;
+        *(int *)dst = c->g.dp;
+        return SISTER_OK;
+    }
+    if (!c->have_intermediates) return c->fail(SISTER_ESTATE, "no computation to inspect");
+    cudaSetDevice(c->device);
+    const Geom &g = c->g;
+    const size_t plane = g.plane;
+    const char *src = nullptr;
+    size_t need = 0;
+    switch (what) {
+    case SISTER_DBG_FRAMES: src = c->frames.as<char>() + (size_t)index * plane; need = plane; break;
+    case SISTER_DBG_CENSUS: src = c->census.as<char>() + (size_t)index * plane * 8; need = plane * 8; break;
+    case SISTER_DBG_WTA: src = c->wta.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
+    case SISTER_DBG_MEDIAN: src = c->med.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
+    case SISTER_DBG_MASKS: src = c->masks.as<char>() + (size_t)index * plane; need = plane; break;
+    case SISTER_DBG_COST: src = c->cost.as<char>(); need = plane * g.dp * 2; break;
+    case SISTER_DBG_SUM0: src = c->sum0.as<char>(); need = plane * g.dp * 2; break;
+    case SISTER_DBG_DISP: src = c->disp.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
+    default: return c->fail(SISTER_EINVAL, "unknown debug item %d", what);
+    }
+    if (index < 0 || index > 7 || bytes < need) return c->fail(SISTER_EINVAL, "bad debug index/size");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(dst, src, need, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return c->cuda_fail(e, "debug fetch");
+    return SISTER_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,78 @@
+"""Regenerate the golden fixtures from the reference's own compiled code (oracle/_ref).
+
+Run from the repository root on an x86-64 host that has the reference tree:
+    python tests/golden/make_golden.py [--c2]
+
+Every case stores the SHA-256 of its five input views (so a test first checks that the seeded
+generator reproduces the same bytes on the machine it runs on) and the reference outputs of the three
+modes of compute_disparities. Small cases also store the inputs themselves.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from sister_gb300 import synth  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def views_sha(views) -> str:
+    h = hashlib.sha256()
+    for v in views:
+        h.update(np.ascontiguousarray(v, np.uint8).tobytes())
+    return h.hexdigest()
+
+
+def out_sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, np.uint16).tobytes()).hexdigest()
+
+
+def small_cases():
+    """(name, views, dc) for the small fixtures: random-texture and synthetic-scene rigs."""
+    rng = np.random.default_rng(20240901)
+    cases = []
+    for (h, w, dc) in [(16, 24, 8), (32, 40, 16), (24, 64, 24)]:
+        cases.append(("rand_%dx%d_dc%d" % (w, h, dc), [rng.integers(0, 256, (h, w), dtype=np.uint8) for _ in range(5)], dc))
+    for k, (w, h, dc) in enumerate([(64, 48, 16), (96, 64, 24), (128, 96, 40), (160, 120, 64), (200, 148, 72),
+                                   (96, 200, 32)]):
+        dmax = max(dc - 8, 6)
+        views, _ = synth.make_rig(w, h, 2, dmax, seed=100 + k, tiles=4)
+        cases.append(("synth_%dx%d_dc%d" % (w, h, dc), views, dc))
+    return cases
+
+
+def main():
+    ref = oracle.Ref()
+    t0 = time.time()
+    for name, views, dc in small_cases():
+        multi, horiz, vert = ref.compute(views, dc)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), views=np.stack(views), dc=dc, multi=multi,
+                            horiz=horiz, vert=vert, views_sha=views_sha(views))
+        print("%-24s %.2fs" % (name, time.time() - t0))
+    (views, gt), dc = synth.rig_c1(1)
+    multi, horiz, vert = ref.compute(views, dc)
+    np.savez_compressed(os.path.join(HERE, "c1_640x480_dc192.npz"), dc=dc, seed=1, views_sha=views_sha(views),
+                        multi_sha=out_sha(multi), horiz_sha=out_sha(horiz), vert_sha=out_sha(vert),
+                        multi_d=(multi // 255).astype(np.uint8), horiz_d=(horiz // 255).astype(np.uint8),
+                        vert_d=(vert // 255).astype(np.uint8))
+    print("c1 %.2fs" % (time.time() - t0))
+    if "--c2" in sys.argv:
+        (views, gt), dc = synth.rig_c2(2)
+        multi, horiz, vert = ref.compute(views, dc)
+        np.savez_compressed(os.path.join(HERE, "c2_1920x1080_dc256.npz"), dc=dc, seed=2, views_sha=views_sha(views),
+                            multi_sha=out_sha(multi), horiz_sha=out_sha(horiz), vert_sha=out_sha(vert),
+                            multi_d=(multi // 255).astype(np.uint8))
+        print("c2 %.2fs" % (time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()

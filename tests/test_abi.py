@@ -1,0 +1,72 @@
+"""CPU checks of the C-ABI library: it builds, loads, exports every symbol include/*.h declares, and fails
+cleanly (status codes, no crash) where no GPU or bad arguments are involved."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+from sister_gb300 import build as sbuild
+import sister_gb300
+
+
+def declared_symbols():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        names += re.findall(r"^\s*SISTER_API\s+(?:int|void|size_t|const char \*)\s*(sister_\w+)\s*\(", src, re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    sbuild.build()
+    return sister_gb300.load_library()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for n in ("sister_ctx_create", "sister_ctx_destroy", "sister_load_views", "sister_set_max_disparity",
+              "sister_compute", "sister_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_only_declared_symbols_are_exported():
+    out = os.popen("nm -D --defined-only %s" % sister_gb300.LIB_PATH).read()
+    exported = set(re.findall(r"\s[TW]\s(sister_\w+)", out))
+    assert exported == set(declared_symbols())
+
+
+def test_null_and_invalid_arguments(lib):
+    assert lib.sister_set_max_disparity(None, 64) == -1
+    assert lib.sister_compute(None, None, None, None) == -1
+    assert lib.sister_ctx_create(None, 0) == -1
+    assert lib.sister_last_error(None) == b"null context"
+
+
+def test_device_bytes_estimate(lib):
+    small = lib.sister_device_bytes(640, 480, 192)
+    big = lib.sister_device_bytes(1920, 1080, 256)
+    assert 0 < small < big
+    # the aggregation volumes dominate: two u16 volumes of (w+2dc)(h+2dc)dc
+    assert big >= 2 * 2 * 2432 * 1592 * 256
+    assert lib.sister_device_bytes(0, 480, 192) == 0
+
+
+def test_no_gpu_context_creation_fails_cleanly(lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert lib.sister_ctx_create(ctypes.byref(h), 0) == -4  # SISTER_EDEVICE
+    with pytest.raises(sister_gb300.SisterError):
+        sister_gb300.Context(0)
