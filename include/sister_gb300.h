@@ -79,6 +79,18 @@ SISTER_API int sister_synchronize(sister_ctx *ctx);
  * (one mode; add the aggregation volume once more per extra mode computed concurrently). */
 SISTER_API size_t sister_device_bytes(int width, int height, int dc);
 
+/* --- tuning: launch-shape knobs of the aggregation kernels (0 = automatic) ------------------- */
+enum {
+    SISTER_TUNE_SGM_ROWS = 1,     /* image rows per CTA (one warp each); 0 = automatic */
+    SISTER_TUNE_SGM_CLUSTER = 2,  /* CTAs per thread-block cluster (1, 2, 4 or 8); 0 = automatic */
+    SISTER_TUNE_SGM_GROUPS = 3,   /* read-only: cluster-sized row groups of the current geometry */
+    SISTER_TUNE_SGM_CLUSTERS = 4  /* read-only: co-resident clusters launched */
+};
+/* Set a knob for subsequent computes (no reference counterpart: the reference is single-threaded CPU code). */
+SISTER_API int sister_tune_set(sister_ctx *ctx, int key, int value);
+/* Read the value in effect for the current geometry (after set_max_disparity and load_views). */
+SISTER_API int sister_tune_get(sister_ctx *ctx, int key, int *value);
+
 /* --- test hooks: intermediates of the last compute (device -> host copies) -------------------- */
 enum {
     SISTER_DBG_FRAMES = 1, /* index k=0..7: frame image k (u8) */

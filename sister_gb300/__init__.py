@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_g
 SISTER_OK = 0
 _ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
 
+TUNE_SGM_ROWS, TUNE_SGM_CLUSTER, TUNE_SGM_GROUPS, TUNE_SGM_CLUSTERS = 1, 2, 3, 4
 DBG_FRAMES, DBG_CENSUS, DBG_WTA, DBG_MEDIAN, DBG_MASKS, DBG_COST, DBG_SUM0, DBG_DISP, DBG_DP = range(1, 10)
 
 
@@ -62,6 +63,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.sister_device_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.sister_device_bytes.restype = ctypes.c_size_t
     lib.sister_debug_fetch.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_size_t]
+    lib.sister_tune_set.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+    lib.sister_tune_get.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     if path is None:
         _lib = lib
     return lib
@@ -125,6 +128,8 @@ class Context:
         self._check(self.lib.sister_set_max_disparity(self.h, int(dc)))
 
     def compute(self, multi=True, horiz=False, vert=False):
+        if self.shape is None:  # nothing loaded: let the library report the call-order error
+            self._check(self.lib.sister_compute(self.h, None, None, None))
         h, w = self.shape
         outs = [np.empty((h, w), np.uint16) if f else None for f in (multi, horiz, vert)]
         ptrs = [o.ctypes.data if o is not None else None for o in outs]
@@ -139,6 +144,18 @@ class Context:
 
     def synchronize(self):
         self._check(self.lib.sister_synchronize(self.h))
+
+    def tune_set(self, key: int, value: int):
+        self._check(self.lib.sister_tune_set(self.h, key, int(value)))
+
+    def tune_get(self, key: int) -> int:
+        v = ctypes.c_int(0)
+        self._check(self.lib.sister_tune_get(self.h, key, ctypes.byref(v)))
+        return v.value
+
+    def plan(self) -> dict:
+        return {k: self.tune_get(v) for k, v in (("rows", TUNE_SGM_ROWS), ("cluster", TUNE_SGM_CLUSTER),
+                                                  ("groups", TUNE_SGM_GROUPS), ("clusters", TUNE_SGM_CLUSTERS))}
 
     def debug(self, what: int, index: int, shape, dtype):
         out = np.empty(shape, dtype)

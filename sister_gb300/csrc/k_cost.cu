@@ -9,7 +9,8 @@ namespace {
 // where (a_f, b_f) are the frame coordinates of (i, j) (hpp:259-261) and C_f is the pair's Hamming cell
 // of census.cpp:54-146: 255 for frame rows 0..2, 0 for the two last rows (never written there), 255 for
 // d > b, else popcount(Cc[a][b] ^ Cn[a][b-d]). Mode 0 uses all frames, 1 frames {0,2}, 2 frames {1,3}.
-// The volume is stored with d-stride dp; entries d >= dc hold 0xFFFF (an infinite cost).
+// The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
+// (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
 // One warp per pixel, lanes over d; 8 pixels of one row per CTA.
 __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__restrict__ census,
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     for (int d = lane; d < g.dp; d += 32) {
         uint32_t s = 0;
         if (d >= D) {
-            s = 0xFFFFu;
+            s = 0x7FFFu;
         } else {
 #pragma unroll
             for (int f = 0; f < 4; f++) {

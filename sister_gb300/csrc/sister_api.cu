@@ -3,6 +3,7 @@
 #include "sister_gb300.h"
 #include "sister_internal.h"
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -60,7 +61,10 @@ struct sister_ctx {
     std::string err;
     bool loaded = false;
     int w = 0, h = 0, dc = 0;
-    DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, bnd, bmin, progress, errflag, disp, outs;
+    DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, bnd, progress, errflag, disp, outs;
+    SgmPlan plan{};
+    int plan_w = 0, plan_h = 0, plan_dc = 0;
+    int tune_rows = 0, tune_cs = 0;
     int last_mode = -1;
     bool have_intermediates = false;
     Geom g{};
@@ -138,10 +142,20 @@ int load_common(sister_ctx *c, const uint8_t *const views[5], int width, int hei
     return SISTER_OK;
 }
 
+const SgmPlan &plan_for(sister_ctx *c, const Geom &g) {
+    if (c->plan_w != g.w || c->plan_h != g.h || c->plan_dc != g.dc) {
+        c->plan = sgm_plan(g, c->device, c->tune_rows, c->tune_cs);
+        c->plan_w = g.w;
+        c->plan_h = g.h;
+        c->plan_dc = g.dc;
+    }
+    return c->plan;
+}
+
 int ensure_buffers(sister_ctx *c, const Geom &g) {
     const size_t plane = g.plane, vol = plane * g.dp;
-    const int R = sgm_rows_per_band(g, c->num_sms);
-    const size_t nb = (size_t)(g.Hp + R - 1) / R;
+    const SgmPlan &p = plan_for(c, g);
+    if (p.R < 1) return c->fail(SISTER_EDEVICE, "no launch configuration fits the aggregation kernel");
     struct {
         DevBuf *b;
         size_t bytes;
@@ -154,9 +168,8 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         {&c->masks, 4 * plane, "masks"},
         {&c->cost, vol * sizeof(uint16_t), "cost volume"},
         {&c->sum0, vol * sizeof(uint16_t), "sum volume"},
-        {&c->bnd, sgm_bnd_elems(g, c->num_sms) * sizeof(uint16_t), "band states"},
-        {&c->bmin, nb * g.Wp * 4 * sizeof(uint16_t), "band minima"},
-        {&c->progress, nb * sizeof(unsigned), "progress"},
+        {&c->bnd, sgm_bnd_bytes(g, p), "group boundary states"},
+        {&c->progress, (size_t)std::max(p.ngroups, 1) * sizeof(unsigned), "progress"},
         {&c->errflag, sizeof(unsigned), "error flag"},
         {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
         {&c->outs, 3 * (size_t)g.w * g.h * sizeof(uint16_t), "outputs"},
@@ -189,7 +202,7 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
-    const int R = sgm_rows_per_band(g, c->num_sms);
+    const SgmPlan &plan = plan_for(c, g);
     for (int mode = 0; mode < 3; mode++) {
         if (!dev_out[mode]) continue;
         launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
@@ -197,7 +210,6 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.cost = c->cost.as<uint16_t>();
         a.sum0 = c->sum0.as<uint16_t>();
         a.bnd = c->bnd.as<uint16_t>();
-        a.bmin = c->bmin.as<uint16_t>();
         a.progress = c->progress.as<unsigned>();
         a.err = c->errflag.as<unsigned>();
         a.out = dev_out[mode];
@@ -209,10 +221,8 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.dc = g.dc;
         a.w = g.w;
         a.h = g.h;
-        a.R = R;
-        a.nbands = (g.Hp + R - 1) / R;
         a.spin_limit = 1u << 22;
-        e = launch_sgm(g, a, st, c->device);
+        e = launch_sgm(g, plan, a, st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->last_mode = mode;
     }
@@ -344,15 +354,44 @@ size_t sister_device_bytes(int width, int height, int dc) {
     if (width <= 0 || height <= 0 || dc <= 0) return 0;
     const Geom g = make_geom(width, height, dc);
     if (g.dpl < 0) return 0;
-    int sms = 152;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaGetLastError();
     const size_t plane = g.plane, vol = plane * g.dp;
-    const int R = sgm_rows_per_band(g, sms);
-    const size_t nb = (size_t)(g.Hp + R - 1) / R;
+    // group boundary records: at most one per band of one row (upper bound without a device query)
+    const size_t bnd = (size_t)g.Hp * g.Wp * (3 * (size_t)g.dp + 8) * 2;
     return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 2 * vol * 2 +
-           sgm_bnd_elems(g, sms) * 2 + nb * g.Wp * 8 + nb * 4 + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+           bnd / 8 + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+}
+
+int sister_tune_set(sister_ctx *c, int key, int value) {
+    if (!c) return SISTER_EINVAL;
+    switch (key) {
+    case SISTER_TUNE_SGM_ROWS:
+        if (value < 0 || value > 16) return c->fail(SISTER_EINVAL, "rows per CTA must be in [0, 16]");
+        c->tune_rows = value;
+        break;
+    case SISTER_TUNE_SGM_CLUSTER:
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+            return c->fail(SISTER_EINVAL, "cluster size must be 0, 1, 2, 4 or 8");
+        c->tune_cs = value;
+        break;
+    default: return c->fail(SISTER_EINVAL, "unknown or read-only tuning key %d", key);
+    }
+    c->plan_w = c->plan_h = c->plan_dc = 0; // re-plan on next use
+    return SISTER_OK;
+}
+
+int sister_tune_get(sister_ctx *c, int key, int *value) {
+    if (!c || !value) return SISTER_EINVAL;
+    if (!c->loaded || !c->dc) return c->fail(SISTER_ESTATE, "load views and set the max disparity first");
+    cudaSetDevice(c->device);
+    const SgmPlan &p = plan_for(c, make_geom(c->w, c->h, c->dc));
+    switch (key) {
+    case SISTER_TUNE_SGM_ROWS: *value = p.R; break;
+    case SISTER_TUNE_SGM_CLUSTER: *value = p.cs; break;
+    case SISTER_TUNE_SGM_GROUPS: *value = p.ngroups; break;
+    case SISTER_TUNE_SGM_CLUSTERS: *value = p.nclusters; break;
+    default: return c->fail(SISTER_EINVAL, "unknown tuning key %d", key);
+    }
+    return SISTER_OK;
 }
 
 int sister_debug_fetch(sister_ctx *c, int what, int index, void *dst, size_t bytes) {

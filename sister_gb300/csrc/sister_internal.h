@@ -20,8 +20,9 @@ struct Geom {
     __host__ __device__ int fcols(int f) const { return (f & 1) ? Hp : Wp; }
 };
 
-// Lanes per pixel are fixed at 32; dpl is chosen from this list (the smallest >= ceil(dc/32)).
-constexpr int kDplChoices[] = {1, 2, 3, 4, 6, 8, 12, 16};
+// Lanes per pixel are fixed at 32; dpl is chosen from this list (the smallest >= ceil(dc/32)); every
+// choice is even so that a lane's slice of a volume row is 4-byte aligned.
+constexpr int kDplChoices[] = {2, 4, 6, 8, 12, 16};
 int choose_dpl(int dc);
 Geom make_geom(int w, int h, int dc);
 
@@ -32,16 +33,21 @@ enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
 struct SgmArgs {
     const uint16_t *cost; // [Hp][Wp][dp] masked multiview cost
     uint16_t *sum0;       // [Hp][Wp][dp] pass-0 path sum (written by pass 0, read by pass 1)
-    uint16_t *bnd;        // [nbands][Wp][3][dp] path states of each band's last row (r1, r2, r3)
-    uint16_t *bmin;       // [nbands][Wp][4] minima of those states
-    unsigned *progress;   // [nbands] pixels of a band's last row published so far
+    uint16_t *bnd;        // [ngroups][Wp][3dp+8] r1/r2/r3 states + minima of each group's last row
+    unsigned *progress;   // [ngroups] pixels of a group's last row published so far
     unsigned *err;        // device error flag
     uint16_t *out;        // [h][w] disparity*255 (pass 1), may be null
     uint16_t *disp;       // [Hp][Wp] padded WTA disparity (pass 1), may be null
     int W, H, D, dp, dc, w, h;
-    int R;                // rows per band (= warps per CTA)
-    int nbands;
-    unsigned spin_limit;  // iterations of the bounded wait before reporting kErrTimeout
+    int R;                // rows per band (= compute warps per CTA)
+    int cs;               // bands per group (= CTAs per cluster)
+    int nbands, ngroups;
+    unsigned spin_limit;  // iterations of a bounded wait before reporting kErrTimeout
+};
+
+// Launch plan of the aggregation kernel for one geometry.
+struct SgmPlan {
+    int R = 0, cs = 0, nbands = 0, ngroups = 0, nclusters = 0;
 };
 
 // one-time per-device kernel attribute setup (dynamic shared memory limits)
@@ -60,8 +66,9 @@ void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStr
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
 // Both aggregation passes plus the final WTA, crop and *255. Returns a cudaError_t.
-cudaError_t launch_sgm(const Geom &g, SgmArgs base, cudaStream_t st, int device);
-int sgm_rows_per_band(const Geom &g, int num_sms);
-size_t sgm_bnd_elems(const Geom &g, int num_sms);
+// force_R / force_cs: 0 = choose automatically
+SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
+size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st);
 
 } // namespace sister
