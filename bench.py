@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the 5-view SiSter disparity path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (N = 1 and per GPU for N > 1): one synthetic 5-view rig, 1920x1080 u8, max disparity 256,
+multiview output (mode 0), the plain single-rig drop-in path. A step is one full compute of that rig.
+Each GPU runs its own replica (the path does not shard; no collective).
+
+Prints one JSON line (rank 0). `value` is Gpix*disp/s (w*h*dc of the unpadded rig per second) with the
+views resident in HBM; `e2e` is the same metric through the public C ABI with pinned host buffers (views
+copied in and the disparity image copied out every step). `--impl reference` times the reference
+algorithm's CPU implementation (the portable C restatement in oracle/, since the reference's SSE code does
+not build on the Arm host) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "5-view Gpix·disp/s and served p50/p99 latency, batched vs plain GPU, bit-exact"
+UNIT = "Gpix*disp/s"
+W_, H_, DC = 1920, 1080, 256
+SEED = 2
+CONFIG = {
+    "workload": "plain single rig: 5 views 1920x1080 u8, maxdisp 256, multiview output (mode 0)",
+    "w": W_, "h": H_, "dc": DC, "seed": SEED,
+    "generator": "seeded synthetic scene: 16 planar tiles + quadratic bump, disparity 10-240 px",
+    "l2": "L2 flushed (256 MB write) before every timed step; cost and sum volumes (2 x 2 GB) exceed L2",
+    "parallelism": "replicas (one rig per GPU per step, no collective)",
+}
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+# kernels of ours launched per compute (frames, census, pair WTA, median, masks, cost, 2 aggregation passes)
+KERNELS_PER_COMPUTE = 8
+
+
+def rig_units() -> float:
+    return W_ * H_ * DC / 1e9
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return PEAKS_FALLBACK["hbm_gbs"], "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(self.NAMES, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, local, world
+
+
+def make_rig():
+    from sister_gb300 import synth
+
+    (views, _), dc = synth.rig_c2(SEED)
+    return views, dc
+
+
+def golden_sha():
+    import numpy as np
+
+    try:
+        z = np.load(os.path.join(ROOT, "tests", "golden", "c2_1920x1080_dc256.npz"))
+        return str(z["multi_sha"])
+    except Exception:
+        return None
+
+
+def cpu_baseline_c2(views, dc):
+    """The oracle on one full rig (mode 0), host cores, wall clock."""
+    import oracle
+
+    port = oracle.Port()
+    t0 = time.perf_counter()
+    port.compute(views, dc, modes=(True, False, False))
+    t = time.perf_counter() - t0
+    return {"value": rig_units() / t, "unit": UNIT, "cores": port.num_threads(), "kind": "port",
+            "sample": "one full 1920x1080/256 rig, mode 0, oracle C restatement (OpenMP), %.1f s" % t}
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    rank, local, world = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from sister_gb300 import build
+
+    build.build()
+    import sister_gb300 as sg
+
+    views, dc = make_rig()
+    h, w = views[0].shape
+    dev_views = [torch.from_numpy(v).cuda() for v in views]
+    out = torch.empty((h, w), dtype=torch.int16, device="cuda")
+    ctx = sg.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.load_views_device([t.data_ptr() for t in dev_views], w, h, w, 1)
+    ctx.set_max_disparity(dc)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # parity guard: the first result must be bit-exact with the reference's golden output
+    ctx.compute_device(out.data_ptr())
+    ctx.synchronize()
+    got = out.cpu().numpy().view(np.uint16)
+    want = golden_sha()
+    bit_exact = (hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest() == want) if want else None
+
+    for _ in range(args.warmup):
+        ctx.compute_device(out.data_ptr())
+    ctx.synchronize()
+    ctx.profile(True)
+    stage_ms = {}
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev[k][0].record(stream)
+        ctx.compute_device(out.data_ptr())
+        ev[k][1].record(stream)
+        for name, ms in ctx.profile_read():
+            stage_ms.setdefault(name, []).append(ms)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ctx.profile(False)
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * rig_units() / (total_ms / 1e3)
+
+    # end to end through the public API: pinned host views in, pinned host disparity out, every step
+    pin_views = [torch.from_numpy(v).pin_memory() for v in views]
+    pin_out = torch.empty((h, w), dtype=torch.int16).pin_memory()
+    ptrs = [t.data_ptr() for t in pin_views]
+    for _ in range(max(2, min(args.warmup, 3))):
+        ctx.load_views_host(ptrs, w, h, w, 1)
+        ctx.compute_host(pin_out.data_ptr())
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.load_views_host(ptrs, w, h, w, 1)
+        ctx.compute_host(pin_out.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_ok = bool((pin_out.numpy().view(np.uint16) == got).all())
+
+    # roofline of the dominant kernel (aggregation passes): algorithmic bytes per launch = cost volume read
+    # (2 B/cell) + pass sum written (pass 0) or read (pass 1) (2 B/cell); cells = (w+2dc)(h+2dc)dc
+    cells = (w + 2 * dc) * (h + 2 * dc) * dc
+    sgm = stage_ms.get("sgm_pass0", []) + stage_ms.get("sgm_pass1", [])
+    peak, peak_kind = load_peaks()
+    roof = None
+    if sgm:
+        avg = sum(sgm) / len(sgm)
+        achieved = 4.0 * cells / (avg / 1e3) / 1e9
+        roof = {"kernel": "sgm_kernel (aggregation pass, avg of pass 0 and 1)", "bound": "hbm", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": 4 * cells, "launch_ms": avg}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": CONFIG,
+            "impl": "gb300", "bit_exact_vs_reference_golden": bit_exact,
+            "e2e": {"value": world * args.steps * rig_units() / e2e_s, "unit": UNIT,
+                    "h2d_bytes_per_step": 5 * w * h, "d2h_bytes_per_step": 2 * w * h, "output_matches": e2e_ok},
+            "gpu_launches": KERNELS_PER_COMPUTE * args.steps,
+            "stage_ms_mean": {k: sum(v) / len(v) for k, v in stage_ms.items()},
+            "roofline": roof, "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline_c2(views, dc)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference algorithm on the host cores (oracle C restatement, all OpenMP threads). Each step
+    processes a rig with the same generator and max disparity; its time is scaled to the full rig by the
+    padded cell count (every stage of the algorithm is linear in (w+2dc)(h+2dc)dc)."""
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from sister_gb300 import synth
+
+    port = oracle.Port()
+    full_cells = (W_ + 2 * DC) * (H_ + 2 * DC) * DC
+
+    def rig(w, h):
+        return synth.make_rig(w, h, 10, 240, seed=SEED, tiles=16, bump=True)[0]
+
+    # calibrate on a small rig, then pick the largest sample that keeps the run within ~3 minutes
+    cal = rig(640, 360)
+    t0 = time.perf_counter()
+    port.compute(cal, DC, modes=(True, False, False))
+    ns_cell = (time.perf_counter() - t0) / ((640 + 2 * DC) * (360 + 2 * DC) * DC)
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    choice = (640, 360)
+    for cand in ((1920, 1080), (1440, 816), (1280, 720), (960, 544), (640, 360)):
+        if ns_cell * (cand[0] + 2 * DC) * (cand[1] + 2 * DC) * DC <= budget:
+            choice = cand
+            break
+    sw, sh = choice
+    views = rig(sw, sh) if choice != (W_, H_) else make_rig()[0]
+    cells = (sw + 2 * DC) * (sh + 2 * DC) * DC
+    for _ in range(args.warmup):
+        port.compute(views, DC, modes=(True, False, False))
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        port.compute(views, DC, modes=(True, False, False))
+        times.append((time.perf_counter() - t0) * full_cells / cells)
+    t_equiv = sum(times) / len(times)
+    value = rig_units() / t_equiv
+    sample = ("%dx%d rig, maxdisp 256, mode 0, same generator; time scaled to 1920x1080 by padded cells (x%.3f)"
+              % (sw, sh, full_cells / cells))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_equiv * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": CONFIG,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": port.num_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference SSE4.1 sources need x86; the host is aarch64, so the portable C restatement "
+                "(bit-exact with the compiled reference) is timed",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -79,6 +79,23 @@ SISTER_API int sister_synchronize(sister_ctx *ctx);
  * (one mode; add the aggregation volume once more per extra mode computed concurrently). */
 SISTER_API size_t sister_device_bytes(int width, int height, int dc);
 
+/* --- stage profiling: CUDA events on the context stream around every stage ----------------- */
+enum {
+    SISTER_STAGE_FRAMES = 1,   /* padded, rotated frame images */
+    SISTER_STAGE_CENSUS = 2,   /* 9x7 census of the eight frame images */
+    SISTER_STAGE_PAIR_WTA = 3, /* per-pair WTA-left/right from census words */
+    SISTER_STAGE_MEDIAN = 4,   /* row-recursive 3x3 medians */
+    SISTER_STAGE_MASKS = 5,    /* LR check and confidence masks */
+    SISTER_STAGE_COST = 6,     /* masked multiview cost volume (once per computed mode) */
+    SISTER_STAGE_SGM0 = 7,     /* aggregation pass 0 (once per computed mode) */
+    SISTER_STAGE_SGM1 = 8      /* aggregation pass 1 + winner-take-all (once per computed mode) */
+};
+/* Enable/disable event recording for subsequent computes (no reference counterpart: the reference only
+ * prints clock() around whole modes, SisterMultiviewDisparities.hpp:73-89). */
+SISTER_API int sister_profile_enable(sister_ctx *ctx, int on);
+/* Durations (ms) and stage ids of the last compute, in launch order; waits for its completion. */
+SISTER_API int sister_profile_read(sister_ctx *ctx, float *ms, int *stage, int max, int *count);
+
 /* --- tuning: launch-shape knobs of the aggregation kernels (0 = automatic) ------------------- */
 enum {
     SISTER_TUNE_SGM_ROWS = 1,     /* image rows per CTA (one warp each); 0 = automatic */

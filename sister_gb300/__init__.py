@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_g
 SISTER_OK = 0
 _ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
 
+STAGES = {1: "frames", 2: "census", 3: "pair_wta", 4: "median", 5: "masks", 6: "cost", 7: "sgm_pass0", 8: "sgm_pass1"}
 TUNE_SGM_ROWS, TUNE_SGM_CLUSTER, TUNE_SGM_GROUPS, TUNE_SGM_CLUSTERS = 1, 2, 3, 4
 DBG_FRAMES, DBG_CENSUS, DBG_WTA, DBG_MEDIAN, DBG_MASKS, DBG_COST, DBG_SUM0, DBG_DISP, DBG_DP = range(1, 10)
 
@@ -63,6 +64,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.sister_device_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.sister_device_bytes.restype = ctypes.c_size_t
     lib.sister_debug_fetch.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_size_t]
+    lib.sister_profile_enable.argtypes = [_vp, ctypes.c_int]
+    lib.sister_profile_read.argtypes = [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]
     lib.sister_tune_set.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
     lib.sister_tune_get.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     if path is None:
@@ -119,6 +123,16 @@ class Context:
         self.shape = (h, w)
         self._keep = vs
 
+    def load_views_host(self, ptrs, width: int, height: int, stride: int, channels: int = 1):
+        """Host pointers (e.g. pinned buffers) in the order center, right, top, left, bottom."""
+        arr = (ctypes.c_void_p * 5)(*[int(p) for p in ptrs])
+        self._check(self.lib.sister_load_views(self.h, arr, width, height, stride, channels))
+        self.shape = (height, width)
+
+    def compute_host(self, multi_ptr=None, horiz_ptr=None, vert_ptr=None):
+        """sister_compute into caller-owned host buffers of width*height u16 (blocking)."""
+        self._check(self.lib.sister_compute(self.h, multi_ptr, horiz_ptr, vert_ptr))
+
     def load_views_device(self, ptrs, width: int, height: int, stride: int, channels: int = 1):
         arr = (ctypes.c_void_p * 5)(*[int(p) for p in ptrs])
         self._check(self.lib.sister_load_views_device(self.h, arr, width, height, stride, channels))
@@ -144,6 +158,17 @@ class Context:
 
     def synchronize(self):
         self._check(self.lib.sister_synchronize(self.h))
+
+    def profile(self, on: bool = True):
+        self._check(self.lib.sister_profile_enable(self.h, int(on)))
+
+    def profile_read(self):
+        """[(stage name, ms), ...] of the last compute, in launch order."""
+        ms = (ctypes.c_float * 64)()
+        st = (ctypes.c_int * 64)()
+        n = ctypes.c_int(0)
+        self._check(self.lib.sister_profile_read(self.h, ms, st, 64, ctypes.byref(n)))
+        return [(STAGES.get(st[k], str(st[k])), float(ms[k])) for k in range(n.value)]
 
     def tune_set(self, key: int, value: int):
         self._check(self.lib.sister_tune_set(self.h, key, int(value)))

@@ -600,35 +600,30 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
     return (size_t)std::max(p.ngroups, 1) * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
 }
 
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st) {
+cudaError_t launch_sgm_pass(const Geom &g, const SgmPlan &p, SgmArgs a, int pass, cudaStream_t st) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
     a.R = p.R;
     a.cs = p.cs;
     a.nbands = p.nbands;
     a.ngroups = p.ngroups;
-    const int threads = (p.R + 2) * 32;
-    for (int pass = 0; pass < 2; pass++) {
-        const void *fn = kernel_for(g.dpl, pass);
-        if (!fn) return cudaErrorInvalidValue;
-        cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
-        if (e != cudaSuccess) return e;
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(p.nclusters * p.cs);
-        cfg.blockDim = dim3(threads);
-        cfg.dynamicSmemBytes = sgm_smem(p.R, g.dp, pass).total;
-        cfg.stream = st;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = p.cs;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        void *args[] = {(void *)&a};
-        e = cudaLaunchKernelExC(&cfg, fn, args);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    const void *fn = kernel_for(g.dpl, pass);
+    if (!fn) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(p.nclusters * p.cs);
+    cfg.blockDim = dim3((p.R + 2) * 32);
+    cfg.dynamicSmemBytes = sgm_smem(p.R, g.dp, pass).total;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = p.cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    void *args[] = {(void *)&a};
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 } // namespace sister

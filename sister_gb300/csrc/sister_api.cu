@@ -65,6 +65,20 @@ struct sister_ctx {
     SgmPlan plan{};
     int plan_w = 0, plan_h = 0, plan_dc = 0;
     int tune_rows = 0, tune_cs = 0;
+    // stage profiling: events recorded on the context stream around every stage of a compute
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_stage; // stage id that ends at event k (k >= 1)
+    void mark(int stage) {
+        if (!prof) return;
+        if (ev.size() <= ev_stage.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+        }
+        cudaEventRecord(ev[ev_stage.size()], stream);
+        ev_stage.push_back(stage);
+    }
     int last_mode = -1;
     bool have_intermediates = false;
     Geom g{};
@@ -195,17 +209,25 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     cudaStream_t st = c->stream;
     cudaError_t e = cudaMemsetAsync(c->errflag.p, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return c->cuda_fail(e, "reset error flag");
+    c->ev_stage.clear();
+    c->mark(-1);
     launch_frames(c->views.as<uint8_t>(), g, c->frames.as<uint8_t>(), st);
+    c->mark(SISTER_STAGE_FRAMES);
     launch_census(c->frames.as<uint8_t>(), g, c->census.as<uint64_t>(), st);
+    c->mark(SISTER_STAGE_CENSUS);
     launch_pair_wta(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), st);
+    c->mark(SISTER_STAGE_PAIR_WTA);
     launch_median(c->wta.as<uint16_t>(), g, c->med.as<uint16_t>(), st);
+    c->mark(SISTER_STAGE_MEDIAN);
     launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
+    c->mark(SISTER_STAGE_MASKS);
     e = cudaGetLastError();
     if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
     const SgmPlan &plan = plan_for(c, g);
     for (int mode = 0; mode < 3; mode++) {
         if (!dev_out[mode]) continue;
         launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
+        c->mark(SISTER_STAGE_COST);
         SgmArgs a{};
         a.cost = c->cost.as<uint16_t>();
         a.sum0 = c->sum0.as<uint16_t>();
@@ -222,8 +244,12 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.w = g.w;
         a.h = g.h;
         a.spin_limit = 1u << 22;
-        e = launch_sgm(g, plan, a, st);
+        e = launch_sgm_pass(g, plan, a, 0, st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
+        c->mark(SISTER_STAGE_SGM0);
+        e = launch_sgm_pass(g, plan, a, 1, st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
+        c->mark(SISTER_STAGE_SGM1);
         c->last_mode = mode;
     }
     c->have_intermediates = true;
@@ -276,6 +302,7 @@ int sister_ctx_create(sister_ctx **out, int device) {
 void sister_ctx_destroy(sister_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
     if (c->own_stream) {
         cudaStreamSynchronize(c->own_stream);
         cudaStreamDestroy(c->own_stream);
@@ -359,6 +386,31 @@ size_t sister_device_bytes(int width, int height, int dc) {
     const size_t bnd = (size_t)g.Hp * g.Wp * (3 * (size_t)g.dp + 8) * 2;
     return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 2 * vol * 2 +
            bnd / 8 + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+}
+
+int sister_profile_enable(sister_ctx *c, int on) {
+    if (!c) return SISTER_EINVAL;
+    c->prof = on != 0;
+    c->ev_stage.clear();
+    return SISTER_OK;
+}
+
+int sister_profile_read(sister_ctx *c, float *ms, int *stage, int max, int *count) {
+    if (!c || !count) return SISTER_EINVAL;
+    *count = 0;
+    if (!c->prof || c->ev_stage.size() < 2) return SISTER_OK;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaEventSynchronize(c->ev[c->ev_stage.size() - 1]);
+    if (e != cudaSuccess) return c->cuda_fail(e, "profile read");
+    int n = 0;
+    for (size_t k = 1; k < c->ev_stage.size() && n < max; k++, n++) {
+        float t = 0;
+        cudaEventElapsedTime(&t, c->ev[k - 1], c->ev[k]);
+        if (ms) ms[n] = t;
+        if (stage) stage[n] = c->ev_stage[k];
+    }
+    *count = n;
+    return SISTER_OK;
 }
 
 int sister_tune_set(sister_ctx *c, int key, int value) {

@@ -69,6 +69,7 @@ void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom
 // force_R / force_cs: 0 = choose automatically
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st);
+// one aggregation pass (0: top-down, stores the pass sum; 1: bottom-up, adds it and reduces)
+cudaError_t launch_sgm_pass(const Geom &g, const SgmPlan &p, SgmArgs a, int pass, cudaStream_t st);
 
 } // namespace sister
