@@ -70,3 +70,31 @@ def test_no_gpu_context_creation_fails_cleanly(lib):
     assert lib.sister_ctx_create(ctypes.byref(h), 0) == -4  # SISTER_EDEVICE
     with pytest.raises(sister_gb300.SisterError):
         sister_gb300.Context(0)
+
+
+def test_cpp_header_compiles_and_links(tmp_path):
+    """The C++ mirror of the reference helper class builds against the library (no GPU needed to link)."""
+    src = tmp_path / "use.cpp"
+    src.write_text('''
+#include "sister_gb300.hpp"
+#include <cstdio>
+int main(int argc, char **argv) {
+    if (argc < 2) { std::printf("%d\\n", (int)sizeof(sister::MultiviewDisparities)); return 0; }
+    std::vector<uint8_t> img(64 * 48, 7);
+    sister::ImageView v{img.data(), 64, 48, 64, 1};
+    try {
+        sister::MultiviewDisparities m(v, v, v, v, v);
+        sister::Image16 multi, horiz, vert;
+        m.compute_disparities(16, &multi, &horiz, &vert);
+    } catch (const sister::Error &e) { std::printf("error %d\\n", e.code()); return 1; }
+    return 0;
+}
+''')
+    exe = tmp_path / "use"
+    libdir = os.path.dirname(sister_gb300.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include", str(src),
+           "-L", libdir, "-lsister_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)]
+    import subprocess
+
+    subprocess.check_call(cmd)
+    assert subprocess.run([str(exe)], capture_output=True).returncode == 0
