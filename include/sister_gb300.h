@@ -79,6 +79,26 @@ SISTER_API int sister_synchronize(sister_ctx *ctx);
  * (one mode; add the aggregation volume once more per extra mode computed concurrently). */
 SISTER_API size_t sister_device_bytes(int width, int height, int dc);
 
+/* --- aggregation without device allocation ------------------------------------------------ */
+/* No counterpart in the reference (which allocates every buffer per call with _mm_malloc).
+ * For callers that cannot allocate device memory when they need a result -- a robot or ROS callback
+ * with a fixed, pre-reserved memory budget and hard latency limits, or code inside a framework that owns
+ * all device allocations. Runs the same 8-path aggregation, winner-take-all, crop and *255 as
+ * sister_compute on a masked cost volume the caller already holds in device memory:
+ *   cost   [(h+2dc)][(w+2dc)][dstride] u16, entries d >= dc set to 0x7FFF (the layout SISTER_DBG_COST
+ *          returns); dstride = 32*k for the smallest k in {2,4,6,8,12,16} with 32*k >= dc
+ *   out    w x h u16 disparity*255 (device, may be NULL); disp_padded (h+2dc) x (w+2dc) u16 (device, may be NULL)
+ * It calls no cudaMalloc/cudaFree: its scratch (pass sum, hand-off records, counters, error flag) lives in
+ * one static device array of SISTER_STATIC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit. Requests needing more return SISTER_EBUDGET with the sizes in `err`. The first call on each device
+ * looks up that array's device address and sets kernel attributes (make that first call before any stream
+ * capture). All calls share the array and it keeps the last call's contents; the call clears what must
+ * start at zero. Calls that overlap on the GPU (other streams, other host threads) race on it. The call
+ * runs on `stream` (NULL: legacy default stream) and returns once the results are written. */
+#define SISTER_STATIC_SCRATCH_BYTES (32u << 20)
+SISTER_API int sister_aggregate_static(const uint16_t *cost, int width, int height, int dc, int dstride, uint16_t *out,
+                                       uint16_t *disp_padded, void *stream, char *err, size_t errlen);
+
 /* --- stage profiling: CUDA events on the context stream around every stage ----------------- */
 enum {
     SISTER_STAGE_FRAMES = 1,   /* padded, rotated frame images */
