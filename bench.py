@@ -113,13 +113,19 @@ def dist_env():
 def make_rig():
     from sister_gb300 import synth
 
-    (views, _), dc = synth.rig_c2(SEED)
-    return views, dc
+    if (W_, H_, DC) == (1920, 1080, 256):
+        (views, _), dc = synth.rig_c2(SEED)
+        return views, dc
+    # other sizes (profiling runs): same generator family, disparities within [10, dc-16]
+    views, _ = synth.make_rig(W_, H_, 10, max(DC - 16, 12), seed=SEED, tiles=16, bump=True)
+    return views, DC
 
 
 def golden_sha():
     import numpy as np
 
+    if (W_, H_, DC) != (1920, 1080, 256):
+        return None
     try:
         z = np.load(os.path.join(ROOT, "tests", "golden", "c2_1920x1080_dc256.npz"))
         return str(z["multi_sha"])
@@ -316,7 +322,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
+    if args.rig:
+        global W_, H_, DC
+        W_, H_, DC = (int(v) for v in args.rig.lower().split("x"))
+        CONFIG.update({"workload": "profiling rig %dx%d maxdisp %d, mode 0" % (W_, H_, DC), "w": W_, "h": H_, "dc": DC})
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
