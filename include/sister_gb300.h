@@ -85,8 +85,8 @@ SISTER_API size_t sister_device_bytes(int width, int height, int dc);
  * with a fixed, pre-reserved memory budget and hard latency limits, or code inside a framework that owns
  * all device allocations. Runs the same 8-path aggregation, winner-take-all, crop and *255 as
  * sister_compute on a masked cost volume the caller already holds in device memory:
- *   cost   [(h+2dc)][(w+2dc)][dstride] u16, entries d >= dc set to 0x7FFF (the layout SISTER_DBG_COST
- *          returns); dstride = 32*k for the smallest k in {2,4,6,8,12,16} with 32*k >= dc
+ *   cost   [(h+2dc)][(w+2dc)][dstride] u16, 16-byte aligned, entries d >= dc set to 0x7FFF (the layout
+ *          SISTER_DBG_COST returns); dstride = 32*k for the smallest k in {2,4,6,8,12,16} with 32*k >= dc
  *   out    w x h u16 disparity*255 (device, may be NULL); disp_padded (h+2dc) x (w+2dc) u16 (device, may be NULL)
  * It calls no cudaMalloc/cudaFree: its scratch (pass sum, hand-off records, counters, error flag) lives in
  * one static device array of SISTER_STATIC_SCRATCH_BYTES that every GPU loading the library holds until

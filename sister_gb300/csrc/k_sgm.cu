@@ -4,24 +4,38 @@
 // The reference runs two raster passes; each pass updates four paths per pixel:
 //   r0 from (i, j-dj), r1 from (i-di, j-dj), r2 from (i-di, j), r3 from (i-di, j+dj)
 // with P1 = 7 and a constant P2 = 100 (adaptP2 with alpha = 0, sgm.cpp:15-22, :34-35). In pass
-// coordinates (row r, column q; pass 1 mirrors both axes) pixel (r, q) depends on (r, q-1), (r-1, q-1),
-// (r-1, q) and (r-1, q+1): a wavefront in which every row trails the row above by two columns.
+// coordinates (row r, column q; pass 1 mirrors both axes) a path value at (r, q) depends on its own
+// predecessor only: r0 on (r, q-1), r1 on (r-1, q-1), r2 on (r-1, q), r3 on (r-1, q+1). The paths are
+// coupled only through the per-pixel sum.
 //
-// Work decomposition
-//   * one warp per image row ("compute warp"), 32 lanes x DPL disparities, sweeping q = 0..W-1;
-//   * R consecutive rows form a band = one CTA; CS consecutive bands form a group = one thread-block
-//     cluster; clusters are persistent and take groups in increasing order;
-//   * a row hands the r1/r2/r3 states of each pixel to the row below through a 4-slot ring of state
-//     records guarded by full/empty mbarriers. Inside a CTA the ring is local shared memory; between
-//     CTAs of a cluster the producer writes straight into the consumer CTA's shared memory (DSMEM) and
-//     arrives on its barrier remotely; between clusters a publisher warp copies the last row of the group
-//     to global memory and releases a progress counter, and a fetcher warp of the next group polls it and
-//     fills that group's first ring. Compute warps never fence or poll global memory.
-//   * the cost volume (and, in pass 1, the pass-0 sum) are prefetched per warp with cp.async, three
-//     pixels ahead.
-// Arithmetic is packed u16x2 (__vminu2 / __vadd2 / __vsub2, all full-rate on sm_103). Real values stay
-// below 1221 so nothing wraps; "infinite" entries (missing columns, disparities >= dc) are 0x7FFF and stay
-// below 0x8064 after any update, so they never win a minimum and never overflow 16 bits.
+// Work decomposition (one CTA = a band of R image rows, persistent over bands)
+//   * four "path warps" per row, one per path, each sweeping q = 0..W-1 with 32 lanes x DPL disparities.
+//     The row-to-row dependency chain (r3 trails the row above by one column) therefore costs one path
+//     update per hop instead of four;
+//   * the r0 warp of a row also owns the row's sum: it gathers r1, r2, r3 of each pixel from the other
+//     three warps, adds r0, and stores the pass-0 sum (pass 0) or finishes the winner-take-all (pass 1);
+//   * the r1, r2, r3 states of a row go to a KP-slot ring with one full barrier per slot (all three path
+//     warps arrive) and one empty barrier per slot (the row's r0 warp and the next row's three path warps
+//     arrive); producers check the empty barriers once per KP/2 pixels;
+//   * data from global memory arrives by bulk copies (TMA). A warp completes about one asynchronous copy
+//     per global-memory round trip however large it is (measured on GB300: ~500-750 cycles per copy for
+//     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows (and in pass 1
+//     the pass-0 sums) of GP consecutive pixels per copy into a two-group ring per row shared by the row's
+//     four warps, one group ahead;
+//   * the last row of a band is handed to the next band through global memory: a collector warp copies
+//     it into a staging ring (so the row never waits on global memory), a writer warp stores the records
+//     and, every FB pixels, fences and releases a progress counter. A fetcher warp of the next band polls
+//     that counter and bulk-copies FB records at a time into a two-batch ring for its first row. In the
+//     first band the fetcher feeds the first line's cost rows to that line's path warps instead (they
+//     need no input), so the slow 8-bit-truncated r0 recurrence of the first line paces no other row.
+//     Compute warps never fence or poll global memory.
+// Arithmetic is packed u16x2: minima with __vminu2, additions and subtractions as plain 32-bit IADDs, which
+// equal packed u16x2 ones whenever no half carries or borrows. That holds on the recurrence: a path value is
+// C + (m - minLp) with minLp <= m <= minLp + 100, so real entries stay below 1021 + 100 and "infinite"
+// entries (missing columns, disparities >= dc, stored as 0x7FFF) below 0x8064 (+7 < 0x10000); m - minLp
+// never borrows since every half of m is >= minLp. Only the 4-path sum of an infinite pair can exceed 16
+// bits; dc is a multiple of 8, so both halves of a pair are real or both infinite, and that carry stays
+// inside a pair whose sums are never read (the final minimum masks d >= dc).
 // Every wait is bounded: on expiry the device error flag is raised and the kernel finishes.
 #include "sister_internal.h"
 
@@ -29,29 +43,46 @@
 
 namespace sister {
 
-constexpr int kCR = 8;    // cost (and pass-0 sum) prefetch ring slots per compute warp
-constexpr int kPF = 3;    // prefetch distance in pixels
-constexpr int kK = 4;     // slots of a row-to-row state ring (power of two)
+constexpr int kHelpers = 3;      // fetcher, collector, writer warps
+constexpr int kRowsMax = 7;      // rows per band for DPL <= 8: 4*7+3 = 31 warps
+constexpr int kRowsMaxWide = 6;  // rows per band for DPL >= 12: 27 warps (register file)
+constexpr int kKP = 4;           // path-ring slots (power of two); producers check empties every kKP/2
+constexpr int kKS = 8;           // staging-ring slots of the band's last row
+// pixels per batched copy: cost group of a row, and records (or first-line cost rows) per fetch
+__host__ __device__ constexpr int batch_px(int dp) { return dp >= 384 ? 4 : 8; }
 
-// One state record: r1 | r2 | r3 (dp u16 each) | minima m1 m2 m3 (+5 pad) -> 6dp + 16 bytes.
+// global hand-off record between bands: r1 | r2 | r3 (dp u16 each) | minima m1 m2 m3 (+5 pad)
 __host__ __device__ inline int rec_u16(int dp) { return 3 * dp + 8; }
+// one path state in a ring slot: state (dp u16) | minimum (+7 pad)
+__host__ __device__ inline int pslot_u16(int dp) { return dp + 8; }
 
 struct SgmSmem {
-    size_t bars, cring, sring, rings, total;
+    size_t bars, prings, inring, stage, cring, sring, total;
+    int nbar;
 };
-// rings 0..R: ring c feeds compute warp c (c < R) or the publisher (c == R)
+// barrier layout (8 bytes each; FB = batch_px(dp), KI = 2*FB):
+//   path ring of row w, slot s: full at 2*(w*kKP + s), empty at +1
+//   incoming ring: batch full barriers [2] at in_base, per-slot empty barriers [KI] after them
+//   staging ring slot s: full at st_base + 2s, empty at +1;  cost group g (0, 1) of row w: c_base + 2w + g
 __host__ __device__ inline SgmSmem sgm_smem(int R, int dp, int pass) {
     SgmSmem L{};
+    const int FB = batch_px(dp), KI = 2 * FB;
+    L.nbar = R * kKP * 2 + 2 + KI + kKS * 2 + R * 2;
     size_t o = 0;
     L.bars = o;
-    o += ((size_t)(R + 1) * kK * 2 + kK) * 8; // full/empty per ring slot, then E_out[kK]
-    o = (o + 15) & ~(size_t)15;
+    o += (size_t)L.nbar * 8;
+    o = (o + 127) & ~(size_t)127;
+    L.prings = o;
+    o += (size_t)R * kKP * 3 * pslot_u16(dp) * 2;
+    L.inring = o;
+    o += (size_t)KI * rec_u16(dp) * 2;
+    L.stage = o;
+    o += (size_t)kKS * rec_u16(dp) * 2;
+    o = (o + 127) & ~(size_t)127;
     L.cring = o;
-    o += (size_t)R * kCR * dp * 2;
+    o += (size_t)R * 2 * FB * dp * 2;
     L.sring = o;
-    if (pass) o += (size_t)R * kCR * dp * 2;
-    L.rings = o;
-    o += (size_t)(R + 1) * kK * rec_u16(dp) * 2;
+    if (pass) o += (size_t)R * 2 * FB * dp * 2;
     L.total = o;
     return L;
 }
@@ -63,29 +94,6 @@ constexpr uint32_t INF2 = 0x7FFF7FFFu;
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t sptr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint32_t cta_rank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t cluster_idx() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t cluster_count() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t mapa(uint32_t saddr, uint32_t rank) {
-    uint32_t r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
-    return r;
-}
-__device__ __forceinline__ void cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -94,54 +102,83 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void cp16(void *sdst, const void *gsrc) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sptr(sdst)), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 __device__ __forceinline__ void mbar_init(uint32_t a, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
 }
 __device__ __forceinline__ void mbar_inval(uint32_t a) {
     asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(a) : "memory");
 }
-__device__ __forceinline__ void mbar_arrive_local(uint32_t a) {
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
 }
-__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+                 : "memory");
 }
-// Bounded wait for phase parity `par`. CLUSTER selects cluster-scope acquire, needed only when the
-// arriving threads live in another CTA of the cluster; CTA scope is much cheaper.
-template <bool CLUSTER>
+// 1D bulk copy global -> shared of this CTA, completion counted on mbarrier `bar`
+// (both addresses 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// non-blocking test of the phase of parity `par`
+__device__ __forceinline__ bool mbar_test(uint32_t a, uint32_t par) {
+    uint32_t ok;
+    asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2; "
+                 "selp.u32 %0, 1, 0, p; }"
+                 : "=r"(ok)
+                 : "r"(a), "r"(par)
+                 : "memory");
+    return ok != 0;
+}
+// blocking test: the warp sleeps until the phase completes or about `ns` nanoseconds pass, so waiting
+// warps take no issue slots from the warps doing the arithmetic
+__device__ __forceinline__ bool mbar_sleep(uint32_t a, uint32_t par, uint32_t ns) {
+    uint32_t ok;
+    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3; "
+                 "selp.u32 %0, 1, 0, p; }"
+                 : "=r"(ok)
+                 : "r"(a), "r"(par), "r"(ns)
+                 : "memory");
+    return ok != 0;
+}
+constexpr uint32_t kSleepNs = 20000; // one blocking test; the error flag and the clock are checked between
+// Bounded wait for the phase of parity `par`: after g.wait_limit_us microseconds, or once another warp has
+// raised the device error flag, the flag is raised and the caller proceeds (the host then reports
+// SISTER_ETIMEOUT), so no wait can hang the GPU.
 __device__ __forceinline__ void mbar_wait(uint32_t a, uint32_t par, const SgmArgs &g) {
-    for (unsigned n = 0;; n++) {
-        uint32_t ok;
-        if constexpr (CLUSTER)
-            asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2; "
-                         "selp.u32 %0, 1, 0, p; }"
-                         : "=r"(ok)
-                         : "r"(a), "r"(par)
-                         : "memory");
-        else
-            asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2; "
-                         "selp.u32 %0, 1, 0, p; }"
-                         : "=r"(ok)
-                         : "r"(a), "r"(par)
-                         : "memory");
-        if (ok) return;
-        if ((n & 1023u) == 1023u && (ld_acquire(g.err) != kErrNone || n > g.spin_limit)) {
+    if (mbar_test(a, par)) return;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        if (mbar_sleep(a, par, kSleepNs)) return;
+        if (ld_acquire(g.err) != kErrNone || global_ns() - t0 > 1000ull * g.wait_limit_us) {
             atomicCAS(g.err, kErrNone, kErrTimeout);
             return;
         }
     }
 }
+// Wait for the phase of parity `par` with a time limit only (no early exit on the error flag): used to
+// drain bulk copies still in flight before barriers are re-initialised or the CTA exits.
+__device__ __forceinline__ void mbar_drain(uint32_t a, uint32_t par, unsigned limit_us) {
+    if (mbar_test(a, par)) return;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_sleep(a, par, kSleepNs) && global_ns() - t0 <= 1000ull * limit_us) {
+    }
+}
+// order this thread's generic-proxy view of global memory (acquired records) before its bulk copies
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 
-// NP consecutive 32-bit words (2*NP u16) from shared memory / to shared memory (local or DSMEM)
+// NP consecutive 32-bit words (2*NP u16) from / to shared or global memory, widest aligned accesses
 template <int NP>
-__device__ __forceinline__ void lds(const uint16_t *p, uint32_t (&o)[NP]) {
+__device__ __forceinline__ void ldw(const uint16_t *p, uint32_t (&o)[NP]) {
     if constexpr (NP % 4 == 0) {
 #pragma unroll
         for (int k = 0; k < NP / 4; k++) {
@@ -160,7 +197,7 @@ __device__ __forceinline__ void lds(const uint16_t *p, uint32_t (&o)[NP]) {
     }
 }
 template <int NP>
-__device__ __forceinline__ void sts_local(uint16_t *p, const uint32_t (&v)[NP]) {
+__device__ __forceinline__ void stw(uint16_t *p, const uint32_t (&v)[NP]) {
     if constexpr (NP % 4 == 0) {
 #pragma unroll
         for (int k = 0; k < NP / 4; k++)
@@ -171,24 +208,6 @@ __device__ __forceinline__ void sts_local(uint16_t *p, const uint32_t (&v)[NP]) 
     } else {
 #pragma unroll
         for (int k = 0; k < NP; k++) reinterpret_cast<uint32_t *>(p)[k] = v[k];
-    }
-}
-template <int NP>
-__device__ __forceinline__ void sts_cluster(uint32_t a, const uint32_t (&v)[NP]) {
-    if constexpr (NP % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < NP / 4; k++)
-            asm volatile("st.shared::cluster.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a + 16 * k), "r"(v[4 * k]),
-                         "r"(v[4 * k + 1]), "r"(v[4 * k + 2]), "r"(v[4 * k + 3])
-                         : "memory");
-    } else if constexpr (NP % 2 == 0) {
-#pragma unroll
-        for (int k = 0; k < NP / 2; k++)
-            asm volatile("st.shared::cluster.v2.u32 [%0], {%1, %2};" ::"r"(a + 8 * k), "r"(v[2 * k]), "r"(v[2 * k + 1])
-                         : "memory");
-    } else {
-#pragma unroll
-        for (int k = 0; k < NP; k++) asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a + 4 * k), "r"(v[k]) : "memory");
     }
 }
 
@@ -212,9 +231,9 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         const uint32_t x = perm_hi_lo(P[k], (k + 1 < NP) ? P[k + 1] : right); // (Lp[d+1], Lp[d+2])
-        const uint32_t t = __vadd2(__vminu2(xprev, x), 0x00070007u);
+        const uint32_t t = __vminu2(xprev, x) + 0x00070007u;
         const uint32_t m = __vminu2(t, __vminu2(P[k], p2));
-        const uint32_t v = __vadd2(C[k], __vsub2(m, m2));
+        const uint32_t v = C[k] + m - m2;
         Ln[k] = v;
         mn = __vminu2(mn, v);
         xprev = x;
@@ -224,285 +243,371 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 
 // ---------------------------------------------------------------- the kernel
 template <int DPL, int PASS>
-__global__ void __launch_bounds__(DPL >= 12 ? 320 : 576) sgm_kernel(const SgmArgs a) {
+__global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + kHelpers) * 32, 1)
+    sgm_kernel(const SgmArgs a) {
     constexpr int NP = DPL / 2;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int R = a.R, W = a.W, H = a.H, dp = a.dp, D = a.D, CS = a.cs;
+    constexpr int KP = kKP, EB = kKP / 2;
+    constexpr int FB = batch_px(32 * DPL); // pixels per batched copy
+    constexpr int KI = 2 * FB;             // incoming-ring slots (two batches)
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int R = a.R, W = a.W, H = a.H, dp = a.dp;
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int d0 = lane * DPL;
-    const int rec = rec_u16(dp);
-    const uint32_t rank = cta_rank();
+    const int rec = rec_u16(dp), ps = pslot_u16(dp);
     const SgmSmem L = sgm_smem(R, dp, PASS);
     const uint32_t bars = sptr(smem + L.bars);
-    auto full_bar = [&](int c, int s) { return bars + (uint32_t)((c * kK + s) * 2) * 8u; };
-    auto empty_bar = [&](int c, int s) { return bars + (uint32_t)((c * kK + s) * 2 + 1) * 8u; };
-    auto eout_bar = [&](int s) { return bars + (uint32_t)((R + 1) * kK * 2 + s) * 8u; };
-    uint16_t *rings = reinterpret_cast<uint16_t *>(smem + L.rings);
-    auto ring_slot = [&](int c, int s) { return rings + (size_t)(c * kK + s) * rec; };
-    const int nbar = (R + 1) * kK * 2 + kK;
+    auto pfull = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s); };
+    auto pempty = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s) + 8u; };
+    const uint32_t in_base = bars + 16u * (uint32_t)(R * KP);
+    auto infull = [&](int b) { return in_base + 8u * (uint32_t)(b & 1); };         // batch b
+    auto inempty = [&](int x) { return in_base + 16u + 8u * (uint32_t)(x & (KI - 1)); }; // pixel x's slot
+    const uint32_t st_base = in_base + 16u + 8u * (uint32_t)KI;
+    auto sfull = [&](int s) { return st_base + 16u * (uint32_t)s; };
+    auto sempty = [&](int s) { return st_base + 16u * (uint32_t)s + 8u; };
+    const uint32_t c_base = st_base + 16u * (uint32_t)kKS;
+    auto cfull = [&](int w, int g) { return c_base + 8u * (uint32_t)(w * 2 + (g & 1)); };
+    uint16_t *prings = reinterpret_cast<uint16_t *>(smem + L.prings);
+    // state of path p (1..3) of row w in slot s
+    auto pslot = [&](int w, int p, int s) { return prings + (size_t)((w * KP + s) * 3 + (p - 1)) * ps; };
+    uint16_t *inring = reinterpret_cast<uint16_t *>(smem + L.inring);
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem + L.stage);
+    uint16_t *cring = reinterpret_cast<uint16_t *>(smem + L.cring);
+    uint16_t *sring = reinterpret_cast<uint16_t *>(smem + L.sring);
 
     // halves holding disparities >= dc are infinite
     uint32_t padm[NP];
 #pragma unroll
     for (int k = 0; k < NP; k++)
-        padm[k] = ((d0 + 2 * k < D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < D) ? 0u : 0xFFFF0000u);
+        padm[k] = ((d0 + 2 * k < a.D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < a.D) ? 0u : 0xFFFF0000u);
 
-    bool first_group = true;
-    for (int grp = (int)cluster_idx(); grp < a.ngroups; grp += (int)cluster_count()) {
-        const int band = grp * CS + (int)rank;
+    // A batch b of FB pixels (q = FB*b ...) covers nb = min(FB, W - FB*b) pixels; in memory (columns j)
+    // they are contiguous, ascending in pass 0 and descending in pass 1. offset of pixel q in its batch:
+    auto boff = [&](int q) {
+        const int t = q % FB;
+        return PASS ? (min(FB, W - (q - t)) - 1 - t) : t;
+    };
+    // first column (lowest j) of batch b, and its pixel count
+    auto bj0 = [&](int b) { return PASS ? max(0, W - FB * (b + 1)) : FB * b; };
+    auto bn = [&](int b) { return min(FB, W - FB * b); };
+
+    const int role = wi / R; // 0: r0 + sum, 1..3: paths r1..r3, then fetcher, collector, writer
+    const int w = wi % R;    // row within the band (compute warps)
+    const int nbat = (W + FB - 1) / FB;
+    bool first_band = true;
+    for (int band = blockIdx.x; band < a.nbands; band += gridDim.x) {
+        const int row0 = band * R;
+        const int rows = min(R, H - row0);
+        const bool publish = rows == R && band + 1 < a.nbands;
         if (threadIdx.x == 0) {
-            for (int k = 0; k < nbar; k++) {
-                const uint32_t b = bars + 8u * k;
-                if (!first_group) mbar_inval(b);
-                mbar_init(b, 32);
+            if (!first_band)
+                for (int k = 0; k < L.nbar; k++) mbar_inval(bars + 8u * k);
+            for (int wr = 0; wr < R; wr++) {
+                // consumers of a row's slots: its r0 warp (32; not on the first line of the pass), plus the next
+                // row's three path warps (96) or, for the band's last row when another band follows, the
+                // collector (32)
+                const unsigned cons = ((row0 + wr == 0) ? 0u : 32u) +
+                                      ((wr + 1 < rows) ? 96u : (wr == R - 1 && publish) ? 32u : 0u);
+                for (int s = 0; s < KP; s++) {
+                    mbar_init(pfull(wr, s), 96);
+                    mbar_init(pempty(wr, s), cons > 0 ? cons : 1);
+                }
+                for (int g = 0; g < 2; g++) mbar_init(cfull(wr, g), 1); // r0's arrive.expect_tx + bytes
+            }
+            for (int b = 0; b < 2; b++) mbar_init(infull(b), 1);    // fetcher's arrive.expect_tx + bytes
+            for (int x = 0; x < KI; x++) mbar_init(inempty(x), 96); // the first row's r1, r2, r3 warps
+            for (int s = 0; s < kKS; s++) {
+                mbar_init(sfull(s), 32);  // collector
+                mbar_init(sempty(s), 32); // writer
             }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
-        first_group = false;
-        cluster_sync();
-        if (band < a.nbands) {
-            const bool has_fetcher = (rank == 0) && (band > 0);
-            const bool has_publisher = (rank == (uint32_t)(CS - 1)) && (band + 1 < a.nbands);
-            if (wi < R) {
-                // ======================================================= compute warp: row r
-                const int r = band * R + wi;
-                if (r < H) {
-                    const int i = PASS ? (H - 1 - r) : r;
-                    const bool first_line = (r == 0);
-                    const size_t rowbase = (size_t)i * W;
-                    // input: ring wi of this CTA; for warp 0 of a non-leading CTA it is written by CTA rank-1
-                    const bool remote_in = (wi == 0) && !first_line && !has_fetcher;
-                    // output: 0 none, 1 local ring wi+1 (next warp or the publisher), 2 ring 0 of CTA rank+1
-                    int omode = 0;
-                    if (r + 1 < H) omode = (wi + 1 < R || has_publisher) ? 1 : 2;
-                    uint16_t *cring = reinterpret_cast<uint16_t *>(smem + L.cring) + (size_t)wi * kCR * dp;
-                    uint16_t *sring = reinterpret_cast<uint16_t *>(smem + L.sring) + (size_t)wi * kCR * dp;
-                    const int chunks = dp / 8;
-                    auto issue = [&](int x) {
-                        if (x < W) {
-                            const size_t pix = rowbase + (PASS ? (W - 1 - x) : x);
-                            const uint16_t *src = a.cost + pix * dp;
-                            uint16_t *dst = cring + (size_t)(x & (kCR - 1)) * dp;
-                            for (int c = lane; c < chunks; c += 32) cp16(dst + 8 * c, src + 8 * c);
-                            if (PASS) {
-                                const uint16_t *s2 = a.sum0 + pix * dp;
-                                uint16_t *d2 = sring + (size_t)(x & (kCR - 1)) * dp;
-                                for (int c = lane; c < chunks; c += 32) cp16(d2 + 8 * c, s2 + 8 * c);
-                            }
-                        }
-                        cp_commit();
-                    };
-                    for (int x = 0; x < kPF; x++) issue(x);
+        first_band = false;
+        __syncthreads();
 
-                    uint32_t r0[NP];
-                    uint32_t r0min = 0;
+        if (role < 4 && w < rows) {
+            const int r = row0 + w;
+            const int i = PASS ? (H - 1 - r) : r;
+            const bool first_line = (r == 0);
+            const size_t rowbase = (size_t)i * W;
+            uint16_t *myc = cring + (size_t)w * 2 * FB * dp;
+            // position of pixel q in the row's cost ring: group (q/FB) & 1
+            auto cidx = [&](int q) { return (size_t)((((q / FB) & 1) * FB) + boff(q)) * dp; };
+            if (role == 0) {
+                // ================================================= r0 warp: cost prefetch, r0, sum, finish
+                uint16_t *mys = sring + (size_t)w * 2 * FB * dp;
+                auto prefetch = [&](int b) {
+                    if (lane == 0 && b < nbat) {
+                        const uint32_t bytes = (uint32_t)(bn(b) * dp * 2);
+                        const size_t pix = rowbase + bj0(b);
+                        const size_t so = (size_t)(b & 1) * FB * dp;
+                        mbar_expect_tx(cfull(w, b), PASS ? 2u * bytes : bytes);
+                        bulk_g2s(sptr(myc + so), a.cost + pix * dp, bytes, cfull(w, b));
+                        if (PASS) bulk_g2s(sptr(mys + so), a.sum0 + pix * dp, bytes, cfull(w, b));
+                    }
+                };
+                prefetch(0);
+                // r0 restarts every row from Lp = 0, minLp = 0 (sgm.cpp:215-216)
+                uint32_t r0[NP];
+                uint32_t r0min = 0;
 #pragma unroll
-                    for (int k = 0; k < NP; k++) r0[k] = INF2;
-
-                    for (int q = 0; q < W; q++) {
-                        cp_wait<kPF - 1>();
-                        __syncwarp();
-                        if (!first_line) {
-                            const uint32_t par1 = ((q + 1) / kK) & 1;
-                            if (remote_in) {
-                                if (q == 0) mbar_wait<true>(full_bar(wi, 0), 0, a);
-                                if (q + 1 < W) mbar_wait<true>(full_bar(wi, (q + 1) & (kK - 1)), par1, a);
-                            } else {
-                                if (q == 0) mbar_wait<false>(full_bar(wi, 0), 0, a);
-                                if (q + 1 < W) mbar_wait<false>(full_bar(wi, (q + 1) & (kK - 1)), par1, a);
-                            }
-                        }
-                        issue(q + kPF);
-                        const int j = PASS ? (W - 1 - q) : q;
-                        uint32_t c[NP];
-                        lds<NP>(cring + (size_t)(q & (kCR - 1)) * dp + d0, c);
-                        uint32_t n1[NP], n2[NP], n3[NP], gsum[NP];
-                        uint32_t mn0, mn1, mn2, mn3;
-                        if (first_line) {
-                            // First line of the pass (sgm.cpp:103-207): C' = (C == 255 ? 0 : C); r1..r3 take
-                            // C' with min C'; r0 starts as C' and then runs the recurrence in int32 truncated to
-                            // 8 bits (saturate_cast<uint16>(uint8), types.h:28); the sum gets r0 alone.
-                            uint32_t cp[NP];
-                            uint32_t mc = 0xFFFFFFFFu;
+                for (int k = 0; k < NP; k++) r0[k] = INF2 & padm[k];
+                for (int q = 0; q < W; q++) {
+                    if (q % FB == 0) {
+                        // group q/FB + 1 reuses the slots of group q/FB - 1, which every warp of the row has
+                        // finished: this warp gathered the path states of its last pixel (on the first line
+                        // this warp is the ring's only reader)
+                        prefetch(q / FB + 1);
+                        mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
+                    }
+                    const size_t ci = cidx(q);
+                    uint32_t c[NP];
+                    ldw<NP>(myc + ci + d0, c);
+                    uint32_t g[NP];
+                    if (first_line) {
+                        // First line (sgm.cpp:103-207): C' = (C == 255 ? 0 : C); r0 starts as C' and then runs the
+                        // recurrence in int32 truncated to 8 bits (saturate_cast<uint16>(uint8), types.h:28);
+                        // the sum receives r0 alone. r1..r3 of the first line only feed the row below.
+                        uint32_t cp[NP];
 #pragma unroll
-                            for (int k = 0; k < NP; k++) {
-                                cp[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
-                                mc = __vminu2(mc, cp[k]);
-                            }
-                            mc = hmin(mc);
-                            if (q == 0) {
-#pragma unroll
-                                for (int k = 0; k < NP; k++) gsum[k] = cp[k];
-                                mn0 = mc;
-                            } else {
-                                uint32_t tmp[NP];
-                                path_step<NP>(r0, r0min, cp, tmp, lane);
-                                uint32_t mnv = 0xFFFFFFFFu;
-#pragma unroll
-                                for (int k = 0; k < NP; k++) {
-                                    const uint32_t v = (tmp[k] & 0x00FF00FFu & ~padm[k]) | (INF2 & padm[k]);
-                                    gsum[k] = v;
-                                    mnv = __vminu2(mnv, v);
-                                }
-                                mn0 = hmin(mnv);
-                            }
+                        for (int k = 0; k < NP; k++) cp[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
+                        uint32_t mnv = 0xFFFFFFFFu;
+                        if (q == 0) {
 #pragma unroll
                             for (int k = 0; k < NP; k++) {
-                                r0[k] = gsum[k];
-                                n1[k] = n2[k] = n3[k] = cp[k];
+                                g[k] = cp[k];
+                                mnv = __vminu2(mnv, cp[k]);
                             }
-                            mn1 = mn2 = mn3 = mc;
                         } else {
-                            // states of the row above: r1 at q-1, r2 at q, r3 at q+1 (missing column: inf, min 0)
-                            uint32_t p1[NP], p2v[NP], p3[NP];
-                            uint32_t m1 = 0, m3 = 0;
-                            if (q > 0) {
-                                const uint16_t *s = ring_slot(wi, (q - 1) & (kK - 1));
-                                lds<NP>(s + d0, p1);
-                                m1 = s[3 * dp + 0];
-                            } else {
-#pragma unroll
-                                for (int k = 0; k < NP; k++) p1[k] = INF2;
-                            }
-                            const uint16_t *s2 = ring_slot(wi, q & (kK - 1));
-                            lds<NP>(s2 + dp + d0, p2v);
-                            const uint32_t m2 = s2[3 * dp + 1];
-                            if (q + 1 < W) {
-                                const uint16_t *s3 = ring_slot(wi, (q + 1) & (kK - 1));
-                                lds<NP>(s3 + 2 * dp + d0, p3);
-                                m3 = s3[3 * dp + 2];
-                            } else {
-#pragma unroll
-                                for (int k = 0; k < NP; k++) p3[k] = INF2;
-                            }
-                            if (q == 0) { // r0 restarts every row from Lp = 0, minLp = 0 (sgm.cpp:215-216)
-#pragma unroll
-                                for (int k = 0; k < NP; k++) r0[k] = INF2 & padm[k];
-                                r0min = 0;
-                            }
-                            uint32_t n0[NP];
-                            mn0 = path_step<NP>(r0, r0min, c, n0, lane);
-                            mn1 = path_step<NP>(p1, m1, c, n1, lane);
-                            mn2 = path_step<NP>(p2v, m2, c, n2, lane);
-                            mn3 = path_step<NP>(p3, m3, c, n3, lane);
+                            uint32_t tmp[NP];
+                            path_step<NP>(r0, r0min, cp, tmp, lane);
 #pragma unroll
                             for (int k = 0; k < NP; k++) {
-                                r0[k] = n0[k];
-                                gsum[k] = __vadd2(__vadd2(n0[k], n1[k]), __vadd2(n2[k], n3[k]));
-                            }
-                            // the slot of column q-1 is no longer needed by this row
-                            if (q >= 1) {
-                                const int s = (q - 1) & (kK - 1);
-                                if (remote_in) mbar_arrive_remote(mapa(eout_bar(s), rank - 1));
-                                else mbar_arrive_local(empty_bar(wi, s));
+                                g[k] = (tmp[k] & 0x00FF00FFu & ~padm[k]) | (INF2 & padm[k]);
+                                mnv = __vminu2(mnv, g[k]);
                             }
                         }
-                        r0min = __reduce_min_sync(FULL, mn0);
-                        // hand r1/r2/r3 of (r, q) to the row below
-                        if (omode) {
-                            const uint32_t v1 = __reduce_min_sync(FULL, mn1);
-                            const uint32_t v2 = __reduce_min_sync(FULL, mn2);
-                            const uint32_t v3 = __reduce_min_sync(FULL, mn3);
-                            const int s = q & (kK - 1);
-                            if (omode == 1) {
-                                if (q >= kK) mbar_wait<false>(empty_bar(wi + 1, s), ((q / kK) - 1) & 1, a);
-                                uint16_t *dst = ring_slot(wi + 1, s);
-                                sts_local<NP>(dst + d0, n1);
-                                sts_local<NP>(dst + dp + d0, n2);
-                                sts_local<NP>(dst + 2 * dp + d0, n3);
-                                if (lane == 0)
-                                    *reinterpret_cast<uint2 *>(dst + 3 * dp) = make_uint2(v1 | (v2 << 16), v3);
-                                mbar_arrive_local(full_bar(wi + 1, s));
-                            } else {
-                                if (q >= kK) mbar_wait<true>(eout_bar(s), ((q / kK) - 1) & 1, a);
-                                const uint32_t dst = mapa(sptr(ring_slot(0, s)), rank + 1);
-                                sts_cluster<NP>(dst + 2u * d0, n1);
-                                sts_cluster<NP>(dst + 2u * (dp + d0), n2);
-                                sts_cluster<NP>(dst + 2u * (2 * dp + d0), n3);
-                                if (lane == 0)
-                                    asm volatile("st.shared::cluster.v2.u32 [%0], {%1, %2};" ::"r"(dst + 6u * dp),
-                                                 "r"(v1 | (v2 << 16)), "r"(v3)
-                                                 : "memory");
-                                mbar_arrive_remote(mapa(full_bar(0, s), rank + 1));
-                            }
+#pragma unroll
+                        for (int k = 0; k < NP; k++) r0[k] = g[k];
+                        r0min = __reduce_min_sync(FULL, hmin(mnv));
+                    } else {
+                        uint32_t n0[NP];
+                        const uint32_t mn = path_step<NP>(r0, r0min, c, n0, lane);
+                        r0min = __reduce_min_sync(FULL, mn);
+                        const int s = q & (KP - 1);
+                        uint32_t v1[NP], v2[NP], v3[NP];
+                        mbar_wait(pfull(w, s), (q / KP) & 1, a);
+                        ldw<NP>(pslot(w, 1, s) + d0, v1);
+                        ldw<NP>(pslot(w, 2, s) + d0, v2);
+                        ldw<NP>(pslot(w, 3, s) + d0, v3);
+                        mbar_arrive(pempty(w, s));
+#pragma unroll
+                        for (int k = 0; k < NP; k++) {
+                            r0[k] = n0[k];
+                            g[k] = n0[k] + v1[k] + v2[k] + v3[k];
                         }
-                        const size_t pix = rowbase + j;
-                        if (PASS == 0) {
-                            sts_local<NP>(a.sum0 + pix * dp + d0, gsum); // generic store to global
-                        } else {
-                            // pass 1 adds to the pass-0 sum (first line: plain u16 add, sgm.cpp:132,:187; else
-                            // saturating, :390 -- neither wraps nor saturates for real disparities), then the
-                            // final WTALeft: lowest d <= min(j, dc-1) of the total (hpp:283, postprocess.cpp:74-185).
-                            uint32_t s0[NP];
-                            lds<NP>(sring + (size_t)(q & (kCR - 1)) * dp + d0, s0);
-                            uint32_t best = 0xFFFFFFFFu;
+                    }
+                    const int j = PASS ? (W - 1 - q) : q;
+                    const size_t pix = rowbase + j;
+                    if (PASS == 0) {
+                        stw<NP>(a.sum0 + pix * dp + d0, g);
+                    } else {
+                        // pass 1 adds to the pass-0 sum (first line: plain u16 add, sgm.cpp:132,:187; else
+                        // saturating, :390 -- neither wraps nor saturates for real disparities), then the final
+                        // WTALeft: lowest d <= min(j, dc-1) of the total (hpp:283, postprocess.cpp:74-185)
+                        uint32_t s0[NP];
+                        ldw<NP>(mys + ci + d0, s0);
+                        // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums
+                        // stay below 2 * 4 * 1121), so they never win
+                        uint32_t sv[NP];
+#pragma unroll
+                        for (int k = 0; k < NP; k++) sv[k] = (s0[k] + g[k]) | padm[k];
+                        if (j < d0 + DPL - 1) {
 #pragma unroll
                             for (int k = 0; k < NP; k++) {
-                                const uint32_t s = __vadd2(s0[k], gsum[k]);
-                                const int d = d0 + 2 * k;
-                                if (d < D && d <= j) best = min(best, ((s & 0xFFFFu) << 16) | (uint32_t)d);
-                                if (d + 1 < D && d + 1 <= j) best = min(best, (s & 0xFFFF0000u) | (uint32_t)(d + 1));
+                                if (d0 + 2 * k > j) sv[k] |= 0x0000FFFFu;
+                                if (d0 + 2 * k + 1 > j) sv[k] |= 0xFFFF0000u;
                             }
-                            best = __reduce_min_sync(FULL, best);
-                            if (lane == 0) {
-                                const uint32_t disp = best & 0xFFFFu;
-                                if (a.disp) a.disp[pix] = (uint16_t)disp;
-                                if (a.out) {
-                                    const int oi = i - a.dc, oj = j - a.dc;
-                                    if (oi >= 0 && oi < a.h && oj >= 0 && oj < a.w)
-                                        a.out[(size_t)oi * a.w + oj] = (uint16_t)min(disp * 255u, 0xFFFFu);
-                                }
+                        }
+                        uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+                        for (int k = 0; k < NP; k++) {
+                            const uint32_t dk = (uint32_t)(d0 + 2 * k);
+                            best = min(best, min(__byte_perm(sv[k], dk, 0x1054), __byte_perm(sv[k], dk + 1u, 0x3254)));
+                        }
+                        best = __reduce_min_sync(FULL, best);
+                        if (lane == 0) {
+                            const uint32_t disp = best & 0xFFFFu;
+                            if (a.disp) a.disp[pix] = (uint16_t)disp;
+                            if (a.out) {
+                                const int oi = i - a.dc, oj = j - a.dc;
+                                if (oi >= 0 && oi < a.h && oj >= 0 && oj < a.w)
+                                    a.out[(size_t)oi * a.w + oj] = (uint16_t)min(disp * 255u, 0xFFFFu);
                             }
                         }
                     }
-                    cp_wait<0>();
                 }
-            } else if (wi == R && has_fetcher) {
-                // ======================================================= fetcher: previous group's last row -> ring 0
-                const uint16_t *src = a.bnd + (size_t)(grp - 1) * W * rec;
-                const unsigned *prog = a.progress + (grp - 1);
-                const int nch = rec / 8; // 16-byte chunks per record
+                // every copy this warp issued has been waited for; after a timeout a wait may have returned
+                // early, so make sure none is still in flight before the barriers are reused
+                if (lane == 0)
+                    for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(cfull(w, b), (b / 2) & 1, a.wait_limit_us);
+            } else {
+                // ================================================= path warp p = role (1: r1, 2: r2, 3: r3)
+                const int p = role;
+                // input: the same path of the row above -- the ring of row w-1, or the incoming ring for w == 0
+                const bool from_in = (w == 0);
+                for (int q = 0; q < W; q++) {
+                    uint32_t c[NP];
+                    if (first_line) {
+                        // the first line's path warps take their cost rows from the fetcher's batches (incoming
+                        // ring), not from the r0 warp's cost ring
+                        if (q % FB == 0) mbar_wait(infull(q / FB), (q / FB / 2) & 1, a);
+                        ldw<NP>(inring + (size_t)((q / FB) & 1) * FB * rec + (size_t)boff(q) * dp + d0, c);
+                        mbar_arrive(inempty(q));
+                    } else {
+                        if (q % FB == 0) mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
+                        ldw<NP>(myc + cidx(q) + d0, c);
+                    }
+                    uint32_t out[NP];
+                    uint32_t mn;
+                    if (first_line) {
+                        // first line: r1..r3 take C' with minimum min(C') (sgm.cpp:112-114, :149-151, :192-194)
+                        uint32_t mnv = 0xFFFFFFFFu;
+#pragma unroll
+                        for (int k = 0; k < NP; k++) {
+                            out[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
+                            mnv = __vminu2(mnv, out[k]);
+                        }
+                        mn = hmin(mnv);
+                    } else {
+                        // r3 reads column q+1 of the row above and never column 0: release that slot unread
+                        if (p == 3 && q == 0) mbar_arrive(from_in ? inempty(0) : pempty(w - 1, 0));
+                        // predecessor column: q-1 (r1), q (r2), q+1 (r3); outside the image: inf with min 0
+                        const int x = q + p - 2;
+                        uint32_t P[NP];
+                        uint32_t mp = 0;
+                        if (x >= 0 && x < W) {
+                            if (from_in) {
+                                // records arrive in batches of FB; consumers take them in order, so a wait at
+                                // the first record of each batch (or the first one this warp reads) suffices
+                                if (x % FB == 0 || x == (p == 3 ? 1 : 0)) mbar_wait(infull(x / FB), (x / FB / 2) & 1, a);
+                                const uint16_t *src = inring + (size_t)(x & (KI - 1)) * rec;
+                                ldw<NP>(src + (size_t)(p - 1) * dp + d0, P);
+                                mp = src[3 * dp + p - 1];
+                                mbar_arrive(inempty(x));
+                            } else {
+                                const int s = x & (KP - 1);
+                                mbar_wait(pfull(w - 1, s), (x / KP) & 1, a);
+                                const uint16_t *src = pslot(w - 1, p, s);
+                                ldw<NP>(src + d0, P);
+                                mp = src[dp];
+                                mbar_arrive(pempty(w - 1, s));
+                            }
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < NP; k++) P[k] = INF2;
+                        }
+                        mn = path_step<NP>(P, mp, c, out, lane);
+                    }
+                    const uint32_t m = __reduce_min_sync(FULL, mn);
+                    // slots q .. q+EB-1 last held pixels q-KP .. q-KP+EB-1; every consumer releases in pixel
+                    // order, so the release of the last of them covers all
+                    if (q >= KP && (q & (EB - 1)) == 0) {
+                        const int y = q - KP + EB - 1;
+                        mbar_wait(pempty(w, y & (KP - 1)), (y / KP) & 1, a);
+                    }
+                    const int s = q & (KP - 1);
+                    uint16_t *dst = pslot(w, p, s);
+                    stw<NP>(dst + d0, out);
+                    if (lane == 0) dst[dp] = (uint16_t)m;
+                    mbar_arrive(pfull(w, s));
+                }
+            }
+        } else if (wi == 4 * R) {
+            // ===================================================== fetcher: batches of FB pixels -> inring
+            // band 0: the first line's cost rows; later bands: the previous band's last-row records
+            if (lane == 0) {
+                const uint16_t *src = a.bnd + (size_t)(band > 0 ? band - 1 : 0) * W * rec;
+                const unsigned *prog = a.progress + (band > 0 ? band - 1 : 0);
+                const size_t rowbase0 = (size_t)(PASS ? H - 1 : 0) * W;
                 unsigned seen = 0;
-                for (int x = 0; x < W; x++) {
-                    const int s = x & (kK - 1);
-                    if (x >= kK) mbar_wait<false>(empty_bar(0, s), ((x / kK) - 1) & 1, a);
-                    if (seen < (unsigned)x + 1u) {
-                        for (unsigned n = 0;; n++) {
+                for (int b = 0; b < nbat; b++) {
+                    // the batch slot last held batch b-2: wait for the release of its last pixel
+                    if (b >= 2) {
+                        const int y = FB * (b - 1) - 1;
+                        mbar_wait(inempty(y), (y / KI) & 1, a);
+                    }
+                    const int nb = bn(b);
+                    uint16_t *dst = inring + (size_t)(b & 1) * FB * rec;
+                    if (band == 0) {
+                        const uint32_t bytes = (uint32_t)(nb * dp * 2);
+                        mbar_expect_tx(infull(b), bytes);
+                        bulk_g2s(sptr(dst), a.cost + (rowbase0 + bj0(b)) * dp, bytes, infull(b));
+                        continue;
+                    }
+                    const unsigned need = (unsigned)(FB * b + nb);
+                    if (seen < need) {
+                        const unsigned long long t0 = global_ns();
+                        for (;;) {
                             const unsigned v = ld_acquire(prog);
-                            if (v >= (unsigned)x + 1u) { seen = v; break; }
-                            if (ld_acquire(a.err) != kErrNone || n > a.spin_limit) {
+                            if (v >= need) {
+                                seen = v;
+                                break;
+                            }
+                            if (ld_acquire(a.err) != kErrNone || global_ns() - t0 > 1000ull * a.wait_limit_us) {
                                 atomicCAS(a.err, kErrNone, kErrTimeout);
                                 seen = 0xFFFFFFFFu;
                                 break;
                             }
                             __nanosleep(64);
                         }
+                        fence_proxy_async_global();
                     }
-                    const uint4 *g4 = reinterpret_cast<const uint4 *>(src + (size_t)x * rec);
-                    uint4 *s4 = reinterpret_cast<uint4 *>(ring_slot(0, s));
-                    for (int k = lane; k < nch; k += 32) s4[k] = __ldcg(g4 + k);
-                    mbar_arrive_local(full_bar(0, s));
+                    const uint32_t bytes = (uint32_t)(nb * rec * 2);
+                    mbar_expect_tx(infull(b), bytes);
+                    bulk_g2s(sptr(dst), src + (size_t)FB * b * rec, bytes, infull(b));
                 }
-            } else if (wi == R + 1 && has_publisher) {
-                // ======================================================= publisher: this group's last row -> global
-                uint16_t *dst = a.bnd + (size_t)grp * W * rec;
-                const int nch = rec / 8;
-                for (int x = 0; x < W; x++) {
-                    const int s = x & (kK - 1);
-                    mbar_wait<false>(full_bar(R, s), (x / kK) & 1, a);
-                    const uint4 *s4 = reinterpret_cast<const uint4 *>(ring_slot(R, s));
-                    uint4 *g4 = reinterpret_cast<uint4 *>(dst + (size_t)x * rec);
-                    for (int k = lane; k < nch; k += 32) g4[k] = s4[k];
-                    mbar_arrive_local(empty_bar(R, s));
-                    if ((x & 7) == 7 || x == W - 1) {
-                        __threadfence();
-                        __syncwarp();
-                        if (lane == 0) st_release(a.progress + grp, (unsigned)(x + 1));
-                    }
+                for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(infull(b), (b / 2) & 1, a.wait_limit_us);
+            }
+        } else if (wi == 4 * R + 1 && publish) {
+            // ===================================================== collector: band's last row -> staging ring
+            const int wl = R - 1;
+            for (int x = 0; x < W; x++) {
+                const int s = x & (kKS - 1);
+                if (x >= kKS) mbar_wait(sempty(s), ((x / kKS) - 1) & 1, a);
+                uint16_t *sd = stage + (size_t)s * rec;
+                const int ks = x & (KP - 1);
+                mbar_wait(pfull(wl, ks), (x / KP) & 1, a);
+                for (int p = 1; p <= 3; p++) {
+                    const uint16_t *sl = pslot(wl, p, ks);
+                    const uint4 *s4 = reinterpret_cast<const uint4 *>(sl);
+                    uint4 *d4 = reinterpret_cast<uint4 *>(sd + (size_t)(p - 1) * dp);
+                    for (int k = lane; k < dp / 8; k += 32) d4[k] = s4[k];
+                    if (lane == 0) sd[3 * dp + p - 1] = sl[dp];
+                }
+                mbar_arrive(pempty(wl, ks));
+                mbar_arrive(sfull(s));
+            }
+        } else if (wi == 4 * R + 2 && publish) {
+            // ===================================================== writer: staging ring -> global, progress
+            uint16_t *dst = a.bnd + (size_t)band * W * rec;
+            const int nch = rec / 8; // 16-byte chunks per record
+            for (int x = 0; x < W; x++) {
+                const int s = x & (kKS - 1);
+                mbar_wait(sfull(s), (x / kKS) & 1, a);
+                const uint4 *s4 = reinterpret_cast<const uint4 *>(stage + (size_t)s * rec);
+                uint4 *g4 = reinterpret_cast<uint4 *>(dst + (size_t)x * rec);
+                for (int k = lane; k < nch; k += 32) g4[k] = s4[k];
+                mbar_arrive(sempty(s));
+                // releases at the end of every fetch batch (the fetcher copies whole batches)
+                if ((x % FB) == FB - 1 || x == W - 1) {
+                    __threadfence();
+                    __syncwarp();
+                    if (lane == 0) st_release(a.progress + band, (unsigned)(x + 1));
                 }
             }
         }
-        cluster_sync();
+        __syncthreads();
     }
 }
 
@@ -528,26 +633,6 @@ const void *kernel_for(int dpl, int pass) {
     }
 }
 
-int max_active_clusters(const void *fn, int cs, int threads, size_t smem) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(cs * 64);
-    cfg.blockDim = dim3(threads);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cs;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
-}
-
 } // namespace
 
 void init_sgm_kernels() {
@@ -559,41 +644,33 @@ void init_sgm_kernels() {
     cudaGetLastError();
 }
 
-SgmPlan sgm_plan(const Geom &g, int device, int force_R, int force_cs) {
-    SgmPlan best{};
+// Rows per band: enough bands to cover the image in one wave of persistent CTAs when it fits
+// (R = ceil(Hp / SMs)), else the largest band the block can hold; force_R overrides (tuning).
+SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands are never clustered*/) {
+    SgmPlan p{};
     int optin = 227 * 1024, sms = 152;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();
-    int rmax = g.dpl >= 12 ? 8 : 16;
+    int rmax = g.dpl >= 12 ? kRowsMaxWide : kRowsMax;
     while (rmax > 1 && sgm_smem(rmax, g.dp, 1).total > (size_t)optin) rmax--;
+    int R = std::max(1, std::min(rmax, (g.Hp + sms - 1) / sms));
+    if (force_R) R = std::max(1, std::min(rmax, force_R));
     const void *fn = kernel_for(g.dpl, 1);
-    if (!fn) return best;
-    for (int cs : {8, 4, 2, 1}) {
-        if (force_cs && cs != force_cs) continue;
-        // co-resident clusters depend on the CTA size, which depends on R: iterate to a fixed point
-        int R = std::max(1, std::min(rmax, (g.Hp + sms - 1) / sms));
-        if (force_R) R = std::max(1, std::min(rmax, force_R));
-        int clusters = 0;
-        for (int it = 0; it < 4; it++) {
-            clusters = max_active_clusters(fn, cs, (R + 2) * 32, sgm_smem(R, g.dp, 1).total);
-            if (clusters < 1 || force_R) break;
-            const int want = (g.Hp + clusters * cs - 1) / (clusters * cs);
-            const int nr = std::max(1, std::min(rmax, want));
-            if (nr == R) break;
-            R = nr;
-        }
-        if (clusters < 1) continue;
-        SgmPlan p{};
-        p.R = R;
-        p.cs = cs;
-        p.nbands = (g.Hp + R - 1) / R;
-        p.ngroups = (p.nbands + cs - 1) / cs;
-        p.nclusters = std::min(p.ngroups, clusters);
-        // prefer fewer rows per CTA (shorter steps), then larger clusters (fewer global hand-offs)
-        if (best.R == 0 || p.R < best.R) best = p;
+    if (!fn) return p;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, g.dp, 1).total) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return p;
     }
-    return best;
+    p.R = R;
+    p.cs = 1;
+    p.nbands = (g.Hp + R - 1) / R;
+    p.ngroups = p.nbands;
+    p.nclusters = std::min(p.nbands, per_sm * sms); // persistent CTAs, all co-resident
+    return p;
 }
 
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
@@ -603,27 +680,17 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
 cudaError_t launch_sgm_pass(const Geom &g, const SgmPlan &p, SgmArgs a, int pass, cudaStream_t st) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
     a.R = p.R;
-    a.cs = p.cs;
+    a.cs = 1;
     a.nbands = p.nbands;
     a.ngroups = p.ngroups;
     const void *fn = kernel_for(g.dpl, pass);
     if (!fn) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
+    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.nbands * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(p.nclusters * p.cs);
-    cfg.blockDim = dim3((p.R + 2) * 32);
-    cfg.dynamicSmemBytes = sgm_smem(p.R, g.dp, pass).total;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = p.cs;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
     void *args[] = {(void *)&a};
-    return cudaLaunchKernelExC(&cfg, fn, args);
+    // cooperative launch: every CTA is resident, so a band never waits on a band that cannot run
+    return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R * 4 + kHelpers) * 32), args,
+                                       sgm_smem(p.R, g.dp, pass).total, st);
 }
 
 } // namespace sister

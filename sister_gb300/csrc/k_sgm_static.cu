@@ -63,6 +63,8 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
                                        size_t errlen) {
     if (err && errlen) err[0] = 0;
     if (!cost) return report(err, errlen, SISTER_EINVAL, "cost volume pointer is NULL");
+    if (reinterpret_cast<uintptr_t>(cost) & 15)
+        return report(err, errlen, SISTER_EINVAL, "cost volume pointer must be 16-byte aligned");
     if (width < 4 || height < 4 || (width % 4) || (height % 4))
         return report(err, errlen, SISTER_EINVAL, "width and height must be positive multiples of 4");
     if (dc < 8 || dc > 512 || (dc % 8))
@@ -112,7 +114,7 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     a.dc = g.dc;
     a.w = g.w;
     a.h = g.h;
-    a.spin_limit = 1u << 22;
+    a.wait_limit_us = 2000000; // 2 s
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the arena keeps the previous call's contents: the error flag must start at zero (the progress
     // counters are cleared by each pass launch)

@@ -243,7 +243,7 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.dc = g.dc;
         a.w = g.w;
         a.h = g.h;
-        a.spin_limit = 1u << 22;
+        a.wait_limit_us = 2000000; // 2 s
         e = launch_sgm_pass(g, plan, a, 0, st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->mark(SISTER_STAGE_SGM0);

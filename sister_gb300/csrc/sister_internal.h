@@ -33,16 +33,16 @@ enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
 struct SgmArgs {
     const uint16_t *cost; // [Hp][Wp][dp] masked multiview cost
     uint16_t *sum0;       // [Hp][Wp][dp] pass-0 path sum (written by pass 0, read by pass 1)
-    uint16_t *bnd;        // [ngroups][Wp][3dp+8] r1/r2/r3 states + minima of each group's last row
-    unsigned *progress;   // [ngroups] pixels of a group's last row published so far
+    uint16_t *bnd;        // [nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row
+    unsigned *progress;   // [nbands] pixels of a band's last row published so far
     unsigned *err;        // device error flag
     uint16_t *out;        // [h][w] disparity*255 (pass 1), may be null
     uint16_t *disp;       // [Hp][Wp] padded WTA disparity (pass 1), may be null
     int W, H, D, dp, dc, w, h;
-    int R;                // rows per band (= compute warps per CTA)
-    int cs;               // bands per group (= CTAs per cluster)
+    int R;                // rows per band (4 path warps per row + fetcher + publisher per CTA)
+    int cs;               // bands per group: always 1 (bands are not clustered)
     int nbands, ngroups;
-    unsigned spin_limit;  // iterations of a bounded wait before reporting kErrTimeout
+    unsigned wait_limit_us; // longest wait of any warp (microseconds) before reporting kErrTimeout
 };
 
 // Launch plan of the aggregation kernel for one geometry.
@@ -66,7 +66,7 @@ void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStr
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
 // Both aggregation passes plus the final WTA, crop and *255. Returns a cudaError_t.
-// force_R / force_cs: 0 = choose automatically
+// force_R: 0 = choose automatically; force_cs is accepted and ignored (groups are single bands)
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
 // one aggregation pass (0: top-down, stores the pass sum; 1: bottom-up, adds it and reduces)
