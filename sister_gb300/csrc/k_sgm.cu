@@ -24,8 +24,9 @@
 //     four warps, one group ahead;
 //   * the last row of a band is handed to the next band through global memory: a collector warp copies
 //     it into a staging ring (so the row never waits on global memory), a writer warp stores the records
-//     and, every FB pixels, fences and releases a progress counter. A fetcher warp of the next band polls
-//     that counter and bulk-copies FB records at a time into a two-batch ring for its first row. In the
+//     and, at the end of every hand-off batch (2, 2, 4 pixels, then FB at a time), fences and releases a
+//     progress counter. A fetcher warp of the next band polls that counter and bulk-copies each batch of
+//     records into a ring of 2*FB slots for its first row, so a band starts two pixels after the one above. In the
 //     first band the fetcher feeds the first line's cost rows to that line's path warps instead (they
 //     need no input), so the slow 8-bit-truncated r0 recurrence of the first line paces no other row.
 //     Compute warps never fence or poll global memory.
@@ -148,18 +149,30 @@ __device__ __forceinline__ bool mbar_sleep(uint32_t a, uint32_t par, uint32_t ns
                  : "memory");
     return ok != 0;
 }
-constexpr uint32_t kSleepNs = 20000; // one blocking test; the error flag and the clock are checked between
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+constexpr uint32_t kSleepNs = 20000; // suspend hint of one blocking test
+constexpr unsigned kCheckEvery = 64; // blocking tests between looks at the error flag and the clock (a
+                                     // global load costs a memory round trip, which would delay every
+                                     // hand-off that just missed its first test)
 // Bounded wait for the phase of parity `par`: after g.wait_limit_us microseconds, or once another warp has
 // raised the device error flag, the flag is raised and the caller proceeds (the host then reports
 // SISTER_ETIMEOUT), so no wait can hang the GPU.
 __device__ __forceinline__ void mbar_wait(uint32_t a, uint32_t par, const SgmArgs &g) {
     if (mbar_test(a, par)) return;
-    const unsigned long long t0 = global_ns();
-    for (;;) {
+    unsigned long long t0 = 0;
+    for (unsigned n = 0;; n++) {
         if (mbar_sleep(a, par, kSleepNs)) return;
-        if (ld_acquire(g.err) != kErrNone || global_ns() - t0 > 1000ull * g.wait_limit_us) {
-            atomicCAS(g.err, kErrNone, kErrTimeout);
-            return;
+        if (n % kCheckEvery == kCheckEvery - 1) {
+            const unsigned long long t = global_ns();
+            if (t0 == 0) t0 = t;
+            if (ld_relaxed(g.err) != kErrNone || t - t0 > 1000ull * g.wait_limit_us) {
+                atomicCAS(g.err, kErrNone, kErrTimeout);
+                return;
+            }
         }
     }
 }
@@ -289,6 +302,14 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     // first column (lowest j) of batch b, and its pixel count
     auto bj0 = [&](int b) { return PASS ? max(0, W - FB * (b + 1)) : FB * b; };
     auto bn = [&](int b) { return min(FB, W - FB * b); };
+    // Hand-off batches of the incoming stream (previous band's records, or the first line's cost rows) start
+    // small so that a band can begin two pixels after the band above: pixels [0,2) [2,4) then doubling up to
+    // FB, then FB at a time (FB = 8: starts 0 2 4 8 16 24 ...). No batch wraps around the ring.
+    constexpr int NPF = (FB == 8) ? 3 : 2; // batches before the first full one
+    auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : FB * (b - NPF + 1); };
+    auto hend = [&](int b) { return min(W, hstart(b + 1)); };
+    auto hbatch = [&](int x) { return x < FB ? (x < 2 ? 0 : 31 - __clz(x)) : x / FB + NPF - 1; };
+    const int nhb = hbatch(W - 1) + 1;
 
     const int role = wi / R; // 0: r0 + sum, 1..3: paths r1..r3, then fetcher, collector, writer
     const int w = wi % R;    // row within the band (compute warps)
@@ -460,9 +481,11 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                     uint32_t c[NP];
                     if (first_line) {
                         // the first line's path warps take their cost rows from the fetcher's batches (incoming
-                        // ring), not from the r0 warp's cost ring
-                        if (q % FB == 0) mbar_wait(infull(q / FB), (q / FB / 2) & 1, a);
-                        ldw<NP>(inring + (size_t)((q / FB) & 1) * FB * rec + (size_t)boff(q) * dp + d0, c);
+                        // ring, row of pixel q at position q % KI, batches stored in memory order), not from the
+                        // r0 warp's cost ring
+                        const int hb = hbatch(q), hs = hstart(hb), he = hend(hb);
+                        if (q == hs) mbar_wait(infull(hb), (hb / 2) & 1, a);
+                        ldw<NP>(inring + (size_t)(hs % KI + (PASS ? he - 1 - q : q - hs)) * dp + d0, c);
                         mbar_arrive(inempty(q));
                     } else {
                         if (q % FB == 0) mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
@@ -488,9 +511,10 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                         uint32_t mp = 0;
                         if (x >= 0 && x < W) {
                             if (from_in) {
-                                // records arrive in batches of FB; consumers take them in order, so a wait at
-                                // the first record of each batch (or the first one this warp reads) suffices
-                                if (x % FB == 0 || x == (p == 3 ? 1 : 0)) mbar_wait(infull(x / FB), (x / FB / 2) & 1, a);
+                                // records arrive in batches; consumers take them in order, so a wait at the first
+                                // record of each batch (or the first one this warp reads) suffices
+                                const int hb = hbatch(x);
+                                if (x == hstart(hb) || x == (p == 3 ? 1 : 0)) mbar_wait(infull(hb), (hb / 2) & 1, a);
                                 const uint16_t *src = inring + (size_t)(x & (KI - 1)) * rec;
                                 ldw<NP>(src + (size_t)(p - 1) * dp + d0, P);
                                 mp = src[3 * dp + p - 1];
@@ -531,43 +555,44 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                 const unsigned *prog = a.progress + (band > 0 ? band - 1 : 0);
                 const size_t rowbase0 = (size_t)(PASS ? H - 1 : 0) * W;
                 unsigned seen = 0;
-                for (int b = 0; b < nbat; b++) {
-                    // the batch slot last held batch b-2: wait for the release of its last pixel
-                    if (b >= 2) {
-                        const int y = FB * (b - 1) - 1;
-                        mbar_wait(inempty(y), (y / KI) & 1, a);
-                    }
-                    const int nb = bn(b);
-                    uint16_t *dst = inring + (size_t)(b & 1) * FB * rec;
+                for (int b = 0; b < nhb; b++) {
+                    const int hs = hstart(b), he = hend(b), nb = he - hs;
+                    // before reusing barrier b & 1 every reader must be past batch b-2, and the ring slots of
+                    // pixels hs..he-1 must be free (they last held pixels hs-KI..he-1-KI); readers release in
+                    // pixel order, so waiting for the later of the two last pixels covers both
+                    const int y = max(b >= 2 ? hend(b - 2) - 1 : -1, he - 1 - KI);
+                    if (y >= 0) mbar_wait(inempty(y), (y / KI) & 1, a);
                     if (band == 0) {
                         const uint32_t bytes = (uint32_t)(nb * dp * 2);
                         mbar_expect_tx(infull(b), bytes);
-                        bulk_g2s(sptr(dst), a.cost + (rowbase0 + bj0(b)) * dp, bytes, infull(b));
+                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), a.cost + (rowbase0 + (PASS ? W - he : hs)) * dp,
+                                 bytes, infull(b));
                         continue;
                     }
-                    const unsigned need = (unsigned)(FB * b + nb);
+                    uint16_t *dst = inring + (size_t)(hs % KI) * rec;
+                    const unsigned need = (unsigned)he;
                     if (seen < need) {
                         const unsigned long long t0 = global_ns();
-                        for (;;) {
+                        for (unsigned n = 0;; n++) {
                             const unsigned v = ld_acquire(prog);
                             if (v >= need) {
                                 seen = v;
                                 break;
                             }
-                            if (ld_acquire(a.err) != kErrNone || global_ns() - t0 > 1000ull * a.wait_limit_us) {
+                            if (n % kCheckEvery == kCheckEvery - 1 &&
+                                (ld_relaxed(a.err) != kErrNone || global_ns() - t0 > 1000ull * a.wait_limit_us)) {
                                 atomicCAS(a.err, kErrNone, kErrTimeout);
                                 seen = 0xFFFFFFFFu;
                                 break;
                             }
-                            __nanosleep(64);
                         }
                         fence_proxy_async_global();
                     }
                     const uint32_t bytes = (uint32_t)(nb * rec * 2);
                     mbar_expect_tx(infull(b), bytes);
-                    bulk_g2s(sptr(dst), src + (size_t)FB * b * rec, bytes, infull(b));
+                    bulk_g2s(sptr(dst), src + (size_t)hs * rec, bytes, infull(b));
                 }
-                for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(infull(b), (b / 2) & 1, a.wait_limit_us);
+                for (int b = max(0, nhb - 2); b < nhb; b++) mbar_drain(infull(b), (b / 2) & 1, a.wait_limit_us);
             }
         } else if (wi == 4 * R + 1 && publish) {
             // ===================================================== collector: band's last row -> staging ring
@@ -599,8 +624,8 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                 uint4 *g4 = reinterpret_cast<uint4 *>(dst + (size_t)x * rec);
                 for (int k = lane; k < nch; k += 32) g4[k] = s4[k];
                 mbar_arrive(sempty(s));
-                // releases at the end of every fetch batch (the fetcher copies whole batches)
-                if ((x % FB) == FB - 1 || x == W - 1) {
+                // releases at the end of every hand-off batch (the fetcher copies whole batches)
+                if (x + 1 == hend(hbatch(x))) {
                     __threadfence();
                     __syncwarp();
                     if (lane == 0) st_release(a.progress + band, (unsigned)(x + 1));
