@@ -6,12 +6,36 @@ namespace sister {
 namespace {
 
 // WTALeft_SSE / WTARight_SSE with uniqueness 1 (postprocess.cpp:74-315) on a pair's Hamming volume
-// (census.cpp:54-146), without materialising the volume. Both reduce to the lowest-index argmin:
-//   L(j) = argmin_{d <= min(j, D-1)} popc(Cc[j] ^ Cn[j-d])
-//   R(j) = argmin_{k <= min(D-1, W-1-j)} popc(Cc[j+k] ^ Cn[j])
+// (census.cpp:54-146), without materialising the volume. Both reduce to the lowest-index argmin of the
+// same keys key(a, b) = popc(Cc[a] ^ Cn[b]) << 16 | (a - b) over the band 0 <= a - b < D:
+//   L(a) = min over b of key(a, b)   (d = a - b <= min(a, D-1))
+//   R(b) = min over a of key(a, b)   (k = a - b <= min(D-1, W-1-b))
+// so every cell is counted once (POPC is the bound). A warp owns 32 consecutive columns b (one per lane)
+// and walks the diagonals d = 0..D-1: lane l meets cell (b0+l+d, b0+l), keeps R of its column in a
+// register, and carries the partial L of row a = b0+l+d, which moves one lane down per step; lane 0's
+// partial is then complete for this block and is merged into a shared array with atomicMin.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
-// One CTA per frame row; both census rows staged in shared memory. Keys pack (cost << 16 | d) so a
-// plain unsigned min yields the lowest-index minimum.
+// One CTA per frame row; both census rows staged in shared memory.
+template <bool EDGE>
+__device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b0, int lane, int W, int dmax,
+                                          uint32_t *lk, uint32_t &racc) {
+    uint32_t lacc = 0xFFFFFFFFu;
+    const int b = b0 + lane;
+#pragma unroll 4
+    for (int d = 0; d < dmax; d++) {
+        const int a = b + d;
+        uint32_t key = 0xFFFFFFFFu;
+        if (!EDGE || a < W) key = ((uint32_t)__popcll(cc[EDGE ? min(a, W - 1) : a] ^ cb) << 16) | (uint32_t)d;
+        racc = min(racc, key);
+        lacc = min(lacc, key);
+        if (lane == 0) atomicMin(&lk[b0 + d], lacc); // a = b0 + d: no later cell of this block
+        lacc = __shfl_down_sync(0xFFFFFFFFu, lacc, 1);
+        if (lane == 31) lacc = 0xFFFFFFFFu;
+    }
+    // lane l now carries row a = b0 + l + dmax, which may still have cells in later diagonals of other blocks
+    if (b + dmax < W && lacc != 0xFFFFFFFFu) atomicMin(&lk[b + dmax], lacc);
+}
+
 __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
                                                        uint16_t *__restrict__ wta) {
     extern __shared__ uint64_t srow[];
@@ -29,25 +53,27 @@ __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restric
         return;
     }
     uint64_t *cc = srow, *cn = srow + W;
+    uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W);
     const uint64_t *gc = census + (size_t)(2 * f) * g.plane + (size_t)i * W;
     const uint64_t *gn = census + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
     for (int j = threadIdx.x; j < W; j += blockDim.x) {
         cc[j] = gc[j];
         cn[j] = gn[j];
+        lk[j] = 0xFFFFFFFFu;
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < W; j += blockDim.x) {
-        const uint64_t a = cc[j];
-        const int endl = min(j, D - 1);
-        uint32_t best = 0xFFFFFFFFu;
-        for (int d = 0; d <= endl; d++) best = min(best, ((uint32_t)__popcll(a ^ cn[j - d]) << 16) | (uint32_t)d);
-        L[j] = (uint16_t)(best & 0xFFFFu);
-        const uint64_t b = cn[j];
-        const int endr = min(D - 1, W - 1 - j);
-        best = 0xFFFFFFFFu;
-        for (int k = 0; k <= endr; k++) best = min(best, ((uint32_t)__popcll(cc[j + k] ^ b) << 16) | (uint32_t)k);
-        R[j] = (uint16_t)(best & 0xFFFFu);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int blk = warp; blk * 32 < W; blk += nw) {
+        const int b0 = 32 * blk, b = b0 + lane;
+        const uint64_t cb = cn[min(b, W - 1)];
+        const int dmax = min(D, W - b0);
+        uint32_t racc = 0xFFFFFFFFu;
+        if (b0 + 31 + dmax - 1 < W) wta_block<false>(cc, cb, b0, lane, W, dmax, lk, racc);
+        else wta_block<true>(cc, cb, b0, lane, W, dmax, lk, racc);
+        if (b < W) R[b] = (uint16_t)(racc & 0xFFFFu);
     }
+    __syncthreads();
+    for (int j = threadIdx.x; j < W; j += blockDim.x) L[j] = (uint16_t)(lk[j] & 0xFFFFu);
 }
 
 // shared ring length for the median sweep: a power of two >= 2W
@@ -81,16 +107,22 @@ __device__ __forceinline__ uint32_t med9(uint32_t v0, uint32_t v1, uint32_t v2, 
 // out[W] = 0; for W < x < N-W-4, out[x] = med9(out[x-W-1], out[x-W], out[x-W+1], in[x-1], in[x], in[x+1],
 // in[x+W-1], in[x+W], in[x+W+1]) where the first three were already filtered in the same sweep.
 // out[x] depends only on positions <= x-W+1, so chunks of W-1 consecutive positions are independent:
-// one CTA sweeps the chunks in order, keeping the last 2W outputs in a shared ring.
+// one CTA per map sweeps the chunks in order, keeping the last 2W outputs in a shared ring. The inputs
+// a chunk reads (positions s-1 .. e+W) are staged in shared memory by cp.async kMedPF chunks ahead into
+// kMedPF+1 buffers, so the sweep never waits on global memory and needs one CTA barrier per chunk.
+constexpr int kMedPF = 3;
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
                                                       uint16_t *__restrict__ med) {
-    extern __shared__ uint16_t ring[]; // ring[x & mask] = out[x] for the last 2W positions
+    extern __shared__ __align__(16) uint16_t msm[];
     const int k = blockIdx.x, f = k >> 1;
     const int H = g.frows(f), W = g.fcols(f);
-    const int N = W * H;
+    const int N = W * H; // a multiple of 16 (W and H are multiples of 4)
     const uint16_t *in = wta + (size_t)k * g.plane;
     uint16_t *out = med + (size_t)k * g.plane;
-    const int mask = median_ring(W) - 1;
+    const int rlen = median_ring(W), mask = rlen - 1;
+    const int blen = 2 * W + 32; // staged input span of one chunk, rounded out to 16-byte boundaries
+    uint16_t *ring = msm;        // ring[x & mask] = out[x] for the last 2W positions
+    uint16_t *bufs = msm + rlen; // kMedPF + 1 staging buffers of blen
     // head: x < W unchanged, x == W -> 0
     for (int x = threadIdx.x; x <= W; x += blockDim.x) {
         const uint16_t v = (x < W) ? in[x] : (uint16_t)0;
@@ -99,19 +131,41 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
     }
     // tail: x >= N-W-4 unchanged
     for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
-    __syncthreads();
     const int end = N - W - 4;
-    for (int s = W + 1; s < end; s += W - 1) {
-        const int e = min(s + W - 1, end);
+    const int per = W - 1;
+    // chunk c covers [W+1 + c*per, min(+per, end)); its inputs span [s-1, e+W+1), staged from base(c)
+    auto base = [&](int sc) { return (sc - 1) & ~7; };
+    auto stage = [&](int sc, uint16_t *dst) {
+        if (sc >= end) return;
+        const int ec = min(sc + per, end);
+        const int b0 = base(sc), b1 = min(N, (ec + W + 1 + 7) & ~7); // b1 <= N - 3 rounded up, N % 8 == 0
+        for (int o = threadIdx.x * 8; b0 + o < b1; o += blockDim.x * 8)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + o)),
+                         "l"(in + b0 + o)
+                         : "memory");
+    };
+    for (int c = 0; c < kMedPF; c++) {
+        stage(W + 1 + c * per, bufs + (size_t)c * blen);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    int c = 0;
+    for (int s = W + 1; s < end; s += per, c++) {
+        asm volatile("cp.async.wait_group %0;" ::"n"(kMedPF - 1) : "memory");
+        // this chunk's inputs (every thread's copies) are in, the previous chunk's outputs are in the ring,
+        // and the buffer of chunk c-1 is free for chunk c+kMedPF
+        __syncthreads();
+        stage(s + kMedPF * per, bufs + (size_t)((c + kMedPF) % (kMedPF + 1)) * blen);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        const int e = min(s + per, end);
+        const uint16_t *bi = bufs + (size_t)(c % (kMedPF + 1)) * blen - base(s); // bi[x] = in[x] for the span
         for (int x = s + threadIdx.x; x < e; x += blockDim.x) {
             const uint32_t v = med9(ring[(x - W - 1) & mask], ring[(x - W) & mask], ring[(x - W + 1) & mask],
-                                    __ldg(in + x - 1), __ldg(in + x), __ldg(in + x + 1),
-                                    __ldg(in + x + W - 1), __ldg(in + x + W), __ldg(in + x + W + 1));
+                                    bi[x - 1], bi[x], bi[x + 1], bi[x + W - 1], bi[x + W], bi[x + W + 1]);
             ring[x & mask] = (uint16_t)v;
             out[x] = (uint16_t)v;
         }
-        __syncthreads();
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) and the mask loops of SisterMultiviewDisparities.hpp:201-251:
@@ -154,13 +208,13 @@ void init_mask_kernels() {
 
 void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t smem = 2 * (size_t)mx * sizeof(uint64_t);
+    const size_t smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
     pair_wta_kernel<<<dim3(mx, 4), 256, smem, st>>>(census, g, wta);
 }
 
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t smem = (size_t)median_ring(mx) * sizeof(uint16_t);
+    const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     median_kernel<<<8, 1024, smem, st>>>(wta, g, med);
 }
 
