@@ -75,8 +75,8 @@ SISTER_API int sister_set_stream(sister_ctx *ctx, void *stream);
 /* Wait for queued work; reports device-side errors (e.g. SISTER_ETIMEOUT) of completed launches. */
 SISTER_API int sister_synchronize(sister_ctx *ctx);
 
-/* Bytes of device memory the context would hold for a w x h rig at max disparity dc
- * (one mode; add the aggregation volume once more per extra mode computed concurrently). */
+/* Bytes of device memory the context would hold for a w x h rig at max disparity dc (about 8.3 GB for
+ * 1920x1080 at 256: cost and two pass-sum volumes of (w+2dc)(h+2dc)*32*ceil(dc/32) u16 dominate). */
 SISTER_API size_t sister_device_bytes(int width, int height, int dc);
 
 /* --- aggregation without device allocation ------------------------------------------------ */
@@ -107,8 +107,8 @@ enum {
     SISTER_STAGE_MEDIAN = 4,   /* row-recursive 3x3 medians */
     SISTER_STAGE_MASKS = 5,    /* LR check and confidence masks */
     SISTER_STAGE_COST = 6,     /* masked multiview cost volume (once per computed mode) */
-    SISTER_STAGE_SGM0 = 7,     /* aggregation pass 0 (once per computed mode) */
-    SISTER_STAGE_SGM1 = 8      /* aggregation pass 1 + winner-take-all (once per computed mode) */
+    SISTER_STAGE_AGGREGATE = 7, /* 8-path aggregation, both passes concurrently (once per computed mode) */
+    SISTER_STAGE_WTA = 8        /* sum of the two passes + winner-take-all, crop, *255 (once per mode) */
 };
 /* Enable/disable event recording for subsequent computes (no reference counterpart: the reference only
  * prints clock() around whole modes, SisterMultiviewDisparities.hpp:73-89). */

@@ -8,20 +8,25 @@
 // predecessor only: r0 on (r, q-1), r1 on (r-1, q-1), r2 on (r-1, q), r3 on (r-1, q+1). The paths are
 // coupled only through the per-pixel sum.
 //
-// Work decomposition (one CTA = a band of R image rows, persistent over bands)
+// The two passes are independent until their sums meet, so one persistent launch runs the bands of both
+// interleaved (work item k: pass k & 1, band k >> 1); each pass stores its 4-path sum and a final
+// memory-bound kernel adds the two sums and takes the winner-take-all. While the bands of one pass wait
+// on the wavefront above them, the other pass's bands keep the SMs busy.
+//
+// Work decomposition (one CTA = a band of R image rows, persistent over work items)
 //   * four "path warps" per row, one per path, each sweeping q = 0..W-1 with 32 lanes x DPL disparities.
 //     The row-to-row dependency chain (r3 trails the row above by one column) therefore costs one path
 //     update per hop instead of four;
 //   * the r0 warp of a row also owns the row's sum: it gathers r1, r2, r3 of each pixel from the other
-//     three warps, adds r0, and stores the pass-0 sum (pass 0) or finishes the winner-take-all (pass 1);
+//     three warps, adds r0, and stores the pass's 4-path sum;
 //   * the r1, r2, r3 states of a row go to a KP-slot ring with one full barrier per slot (all three path
 //     warps arrive) and one empty barrier per slot (the row's r0 warp and the next row's three path warps
 //     arrive); producers check the empty barriers once per KP/2 pixels;
 //   * data from global memory arrives by bulk copies (TMA). A warp completes about one asynchronous copy
 //     per global-memory round trip however large it is (measured on GB300: ~500-750 cycles per copy for
-//     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows (and in pass 1
-//     the pass-0 sums) of GP consecutive pixels per copy into a two-group ring per row shared by the row's
-//     four warps, one group ahead;
+//     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows of FB
+//     consecutive pixels per copy into a two-group ring per row shared by the row's four warps, one group
+//     ahead;
 //   * the last row of a band is handed to the next band through global memory: a collector warp copies
 //     it into a staging ring (so the row never waits on global memory), a writer warp stores the records
 //     and, at the end of every hand-off batch (2, 2, 4 pixels, then FB at a time), fences and releases a
@@ -47,10 +52,11 @@ namespace sister {
 constexpr int kHelpers = 3;      // fetcher, collector, writer warps
 constexpr int kRowsMax = 7;      // rows per band for DPL <= 8: 4*7+3 = 31 warps
 constexpr int kRowsMaxWide = 6;  // rows per band for DPL >= 12: 27 warps (register file)
-constexpr int kKP = 4;           // path-ring slots (power of two); producers check empties every kKP/2
 constexpr int kKS = 8;           // staging-ring slots of the band's last row
 // pixels per batched copy: cost group of a row, and records (or first-line cost rows) per fetch
 __host__ __device__ constexpr int batch_px(int dp) { return dp >= 384 ? 4 : 8; }
+// path-ring slots (power of two; producers check the empty barriers every half ring)
+__host__ __device__ constexpr int path_slots(int dp) { return dp >= 384 ? 4 : 8; }
 
 // global hand-off record between bands: r1 | r2 | r3 (dp u16 each) | minima m1 m2 m3 (+5 pad)
 __host__ __device__ inline int rec_u16(int dp) { return 3 * dp + 8; }
@@ -58,23 +64,23 @@ __host__ __device__ inline int rec_u16(int dp) { return 3 * dp + 8; }
 __host__ __device__ inline int pslot_u16(int dp) { return dp + 8; }
 
 struct SgmSmem {
-    size_t bars, prings, inring, stage, cring, sring, total;
+    size_t bars, prings, inring, stage, cring, total;
     int nbar;
 };
-// barrier layout (8 bytes each; FB = batch_px(dp), KI = 2*FB):
-//   path ring of row w, slot s: full at 2*(w*kKP + s), empty at +1
+// barrier layout (8 bytes each; FB = batch_px(dp), KI = 2*FB, KP = path_slots(dp)):
+//   path ring of row w, slot s: full at 2*(w*KP + s), empty at +1
 //   incoming ring: batch full barriers [2] at in_base, per-slot empty barriers [KI] after them
 //   staging ring slot s: full at st_base + 2s, empty at +1;  cost group g (0, 1) of row w: c_base + 2w + g
-__host__ __device__ inline SgmSmem sgm_smem(int R, int dp, int pass) {
+__host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
     SgmSmem L{};
-    const int FB = batch_px(dp), KI = 2 * FB;
-    L.nbar = R * kKP * 2 + 2 + KI + kKS * 2 + R * 2;
+    const int FB = batch_px(dp), KI = 2 * FB, KP = path_slots(dp);
+    L.nbar = R * KP * 2 + 2 + KI + kKS * 2 + R * 2;
     size_t o = 0;
     L.bars = o;
     o += (size_t)L.nbar * 8;
     o = (o + 127) & ~(size_t)127;
     L.prings = o;
-    o += (size_t)R * kKP * 3 * pslot_u16(dp) * 2;
+    o += (size_t)R * KP * 3 * pslot_u16(dp) * 2;
     L.inring = o;
     o += (size_t)KI * rec_u16(dp) * 2;
     L.stage = o;
@@ -82,8 +88,6 @@ __host__ __device__ inline SgmSmem sgm_smem(int R, int dp, int pass) {
     o = (o + 127) & ~(size_t)127;
     L.cring = o;
     o += (size_t)R * 2 * FB * dp * 2;
-    L.sring = o;
-    if (pass) o += (size_t)R * 2 * FB * dp * 2;
     L.total = o;
     return L;
 }
@@ -255,11 +259,11 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 }
 
 // ---------------------------------------------------------------- the kernel
-template <int DPL, int PASS>
+template <int DPL>
 __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + kHelpers) * 32, 1)
     sgm_kernel(const SgmArgs a) {
     constexpr int NP = DPL / 2;
-    constexpr int KP = kKP, EB = kKP / 2;
+    constexpr int KP = path_slots(32 * DPL), EB = KP / 2;
     constexpr int FB = batch_px(32 * DPL); // pixels per batched copy
     constexpr int KI = 2 * FB;             // incoming-ring slots (two batches)
     extern __shared__ __align__(128) unsigned char smem[];
@@ -267,7 +271,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int d0 = lane * DPL;
     const int rec = rec_u16(dp), ps = pslot_u16(dp);
-    const SgmSmem L = sgm_smem(R, dp, PASS);
+    const SgmSmem L = sgm_smem(R, dp);
     const uint32_t bars = sptr(smem + L.bars);
     auto pfull = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s); };
     auto pempty = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s) + 8u; };
@@ -285,7 +289,6 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     uint16_t *inring = reinterpret_cast<uint16_t *>(smem + L.inring);
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem + L.stage);
     uint16_t *cring = reinterpret_cast<uint16_t *>(smem + L.cring);
-    uint16_t *sring = reinterpret_cast<uint16_t *>(smem + L.sring);
 
     // halves holding disparities >= dc are infinite
     uint32_t padm[NP];
@@ -293,14 +296,15 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     for (int k = 0; k < NP; k++)
         padm[k] = ((d0 + 2 * k < a.D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < a.D) ? 0u : 0xFFFF0000u);
 
+    int pass = 0; // pass of the current work item: 0 top-down left-to-right, 1 mirrored
     // A batch b of FB pixels (q = FB*b ...) covers nb = min(FB, W - FB*b) pixels; in memory (columns j)
     // they are contiguous, ascending in pass 0 and descending in pass 1. offset of pixel q in its batch:
     auto boff = [&](int q) {
         const int t = q % FB;
-        return PASS ? (min(FB, W - (q - t)) - 1 - t) : t;
+        return pass ? (min(FB, W - (q - t)) - 1 - t) : t;
     };
     // first column (lowest j) of batch b, and its pixel count
-    auto bj0 = [&](int b) { return PASS ? max(0, W - FB * (b + 1)) : FB * b; };
+    auto bj0 = [&](int b) { return pass ? max(0, W - FB * (b + 1)) : FB * b; };
     auto bn = [&](int b) { return min(FB, W - FB * b); };
     // Hand-off batches of the incoming stream (previous band's records, or the first line's cost rows) start
     // small so that a band can begin two pixels after the band above: pixels [0,2) [2,4) then doubling up to
@@ -315,7 +319,12 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     const int w = wi % R;    // row within the band (compute warps)
     const int nbat = (W + FB - 1) / FB;
     bool first_band = true;
-    for (int band = blockIdx.x; band < a.nbands; band += gridDim.x) {
+    for (int item = blockIdx.x; item < 2 * a.nbands; item += gridDim.x) {
+        pass = item & 1;
+        const int band = item >> 1;
+        uint16_t *sum = pass ? a.sum1 : a.sum0;
+        uint16_t *bnd = a.bnd + (size_t)pass * a.nbands * W * rec;
+        unsigned *progress = a.progress + (size_t)pass * a.nbands;
         const int row0 = band * R;
         const int rows = min(R, H - row0);
         const bool publish = rows == R && band + 1 < a.nbands;
@@ -348,23 +357,20 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
 
         if (role < 4 && w < rows) {
             const int r = row0 + w;
-            const int i = PASS ? (H - 1 - r) : r;
+            const int i = pass ? (H - 1 - r) : r;
             const bool first_line = (r == 0);
             const size_t rowbase = (size_t)i * W;
             uint16_t *myc = cring + (size_t)w * 2 * FB * dp;
             // position of pixel q in the row's cost ring: group (q/FB) & 1
             auto cidx = [&](int q) { return (size_t)((((q / FB) & 1) * FB) + boff(q)) * dp; };
             if (role == 0) {
-                // ================================================= r0 warp: cost prefetch, r0, sum, finish
-                uint16_t *mys = sring + (size_t)w * 2 * FB * dp;
+                // ================================================= r0 warp: cost prefetch, r0, sum
                 auto prefetch = [&](int b) {
                     if (lane == 0 && b < nbat) {
                         const uint32_t bytes = (uint32_t)(bn(b) * dp * 2);
                         const size_t pix = rowbase + bj0(b);
-                        const size_t so = (size_t)(b & 1) * FB * dp;
-                        mbar_expect_tx(cfull(w, b), PASS ? 2u * bytes : bytes);
-                        bulk_g2s(sptr(myc + so), a.cost + pix * dp, bytes, cfull(w, b));
-                        if (PASS) bulk_g2s(sptr(mys + so), a.sum0 + pix * dp, bytes, cfull(w, b));
+                        mbar_expect_tx(cfull(w, b), bytes);
+                        bulk_g2s(sptr(myc + (size_t)(b & 1) * FB * dp), a.cost + pix * dp, bytes, cfull(w, b));
                     }
                 };
                 prefetch(0);
@@ -428,45 +434,9 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                             g[k] = n0[k] + v1[k] + v2[k] + v3[k];
                         }
                     }
-                    const int j = PASS ? (W - 1 - q) : q;
-                    const size_t pix = rowbase + j;
-                    if (PASS == 0) {
-                        stw<NP>(a.sum0 + pix * dp + d0, g);
-                    } else {
-                        // pass 1 adds to the pass-0 sum (first line: plain u16 add, sgm.cpp:132,:187; else
-                        // saturating, :390 -- neither wraps nor saturates for real disparities), then the final
-                        // WTALeft: lowest d <= min(j, dc-1) of the total (hpp:283, postprocess.cpp:74-185)
-                        uint32_t s0[NP];
-                        ldw<NP>(mys + ci + d0, s0);
-                        // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums
-                        // stay below 2 * 4 * 1121), so they never win
-                        uint32_t sv[NP];
-#pragma unroll
-                        for (int k = 0; k < NP; k++) sv[k] = (s0[k] + g[k]) | padm[k];
-                        if (j < d0 + DPL - 1) {
-#pragma unroll
-                            for (int k = 0; k < NP; k++) {
-                                if (d0 + 2 * k > j) sv[k] |= 0x0000FFFFu;
-                                if (d0 + 2 * k + 1 > j) sv[k] |= 0xFFFF0000u;
-                            }
-                        }
-                        uint32_t best = 0xFFFFFFFFu;
-#pragma unroll
-                        for (int k = 0; k < NP; k++) {
-                            const uint32_t dk = (uint32_t)(d0 + 2 * k);
-                            best = min(best, min(__byte_perm(sv[k], dk, 0x1054), __byte_perm(sv[k], dk + 1u, 0x3254)));
-                        }
-                        best = __reduce_min_sync(FULL, best);
-                        if (lane == 0) {
-                            const uint32_t disp = best & 0xFFFFu;
-                            if (a.disp) a.disp[pix] = (uint16_t)disp;
-                            if (a.out) {
-                                const int oi = i - a.dc, oj = j - a.dc;
-                                if (oi >= 0 && oi < a.h && oj >= 0 && oj < a.w)
-                                    a.out[(size_t)oi * a.w + oj] = (uint16_t)min(disp * 255u, 0xFFFFu);
-                            }
-                        }
-                    }
+                    // the pass's sum: first line r0 alone (sgm.cpp:132, :187), else r0+r1+r2+r3 (:386-391); u16
+                    // arithmetic never saturates or wraps for real disparities
+                    stw<NP>(sum + (rowbase + (pass ? (W - 1 - q) : q)) * dp + d0, g);
                 }
                 // every copy this warp issued has been waited for; after a timeout a wait may have returned
                 // early, so make sure none is still in flight before the barriers are reused
@@ -485,7 +455,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                         // r0 warp's cost ring
                         const int hb = hbatch(q), hs = hstart(hb), he = hend(hb);
                         if (q == hs) mbar_wait(infull(hb), (hb / 2) & 1, a);
-                        ldw<NP>(inring + (size_t)(hs % KI + (PASS ? he - 1 - q : q - hs)) * dp + d0, c);
+                        ldw<NP>(inring + (size_t)(hs % KI + (pass ? he - 1 - q : q - hs)) * dp + d0, c);
                         mbar_arrive(inempty(q));
                     } else {
                         if (q % FB == 0) mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
@@ -551,9 +521,9 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
             // ===================================================== fetcher: batches of FB pixels -> inring
             // band 0: the first line's cost rows; later bands: the previous band's last-row records
             if (lane == 0) {
-                const uint16_t *src = a.bnd + (size_t)(band > 0 ? band - 1 : 0) * W * rec;
-                const unsigned *prog = a.progress + (band > 0 ? band - 1 : 0);
-                const size_t rowbase0 = (size_t)(PASS ? H - 1 : 0) * W;
+                const uint16_t *src = bnd + (size_t)(band > 0 ? band - 1 : 0) * W * rec;
+                const unsigned *prog = progress + (band > 0 ? band - 1 : 0);
+                const size_t rowbase0 = (size_t)(pass ? H - 1 : 0) * W;
                 unsigned seen = 0;
                 for (int b = 0; b < nhb; b++) {
                     const int hs = hstart(b), he = hend(b), nb = he - hs;
@@ -565,7 +535,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                     if (band == 0) {
                         const uint32_t bytes = (uint32_t)(nb * dp * 2);
                         mbar_expect_tx(infull(b), bytes);
-                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), a.cost + (rowbase0 + (PASS ? W - he : hs)) * dp,
+                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), a.cost + (rowbase0 + (pass ? W - he : hs)) * dp,
                                  bytes, infull(b));
                         continue;
                     }
@@ -615,7 +585,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
             }
         } else if (wi == 4 * R + 2 && publish) {
             // ===================================================== writer: staging ring -> global, progress
-            uint16_t *dst = a.bnd + (size_t)band * W * rec;
+            uint16_t *dst = bnd + (size_t)band * W * rec;
             const int nch = rec / 8; // 16-byte chunks per record
             for (int x = 0; x < W; x++) {
                 const int s = x & (kKS - 1);
@@ -628,7 +598,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                 if (x + 1 == hend(hbatch(x))) {
                     __threadfence();
                     __syncwarp();
-                    if (lane == 0) st_release(a.progress + band, (unsigned)(x + 1));
+                    if (lane == 0) st_release(progress + band, (unsigned)(x + 1));
                 }
             }
         }
@@ -636,24 +606,49 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     }
 }
 
+// Sum of the two passes' sums and the final WTALeft (hpp:283, postprocess.cpp:74-185): the lowest
+// d <= min(j, dc-1) of S0 + S1 (pass 1 adds its sum to pass 0's, saturating at sgm.cpp:390 -- real sums
+// stay below 2 * 4 * 1121, so nothing saturates), then crop and *255 (hpp:111-118). One warp per padded
+// pixel, lanes over d; memory-bound (reads both sum volumes once).
 template <int DPL>
-void set_attrs(int optin) {
-    cudaFuncSetAttribute(sgm_kernel<DPL, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    cudaFuncSetAttribute(sgm_kernel<DPL, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+__global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict__ s0v, const uint16_t *__restrict__ s1v,
+                                                      Geom g, uint16_t *__restrict__ out, uint16_t *__restrict__ disp) {
+    constexpr int NP = DPL / 2;
+    const int lane = threadIdx.x & 31;
+    const size_t pix = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (pix >= g.plane) return;
+    const int i = (int)(pix / g.Wp), j = (int)(pix % g.Wp);
+    const int d0 = lane * DPL, D = g.dc;
+    uint32_t s0[NP], s1[NP];
+    ldw<NP>(s0v + pix * g.dp + d0, s0);
+    ldw<NP>(s1v + pix * g.dp + d0, s1);
+    // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums are smaller)
+    uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const int d = d0 + 2 * k;
+        uint32_t sv = s0[k] + s1[k]; // both halves of a pair are real or both infinite (dc % 8 == 0)
+        if (d >= D || d > j) sv |= 0x0000FFFFu;
+        if (d + 1 >= D || d + 1 > j) sv |= 0xFFFF0000u;
+        best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+    }
+    best = __reduce_min_sync(FULL, best);
+    if (lane == 0) {
+        const uint32_t dv = best & 0xFFFFu;
+        if (disp) disp[pix] = (uint16_t)dv;
+        const int oi = i - g.dc, oj = j - g.dc;
+        if (out && oi >= 0 && oi < g.h && oj >= 0 && oj < g.w) out[(size_t)oi * g.w + oj] = (uint16_t)min(dv * 255u, 0xFFFFu);
+    }
 }
 
-template <int DPL>
-const void *kernel_ptr(int pass) {
-    return pass ? (const void *)sgm_kernel<DPL, 1> : (const void *)sgm_kernel<DPL, 0>;
-}
-const void *kernel_for(int dpl, int pass) {
+const void *kernel_for(int dpl) {
     switch (dpl) {
-    case 2: return kernel_ptr<2>(pass);
-    case 4: return kernel_ptr<4>(pass);
-    case 6: return kernel_ptr<6>(pass);
-    case 8: return kernel_ptr<8>(pass);
-    case 12: return kernel_ptr<12>(pass);
-    case 16: return kernel_ptr<16>(pass);
+    case 2: return (const void *)sgm_kernel<2>;
+    case 4: return (const void *)sgm_kernel<4>;
+    case 6: return (const void *)sgm_kernel<6>;
+    case 8: return (const void *)sgm_kernel<8>;
+    case 12: return (const void *)sgm_kernel<12>;
+    case 16: return (const void *)sgm_kernel<16>;
     default: return nullptr;
     }
 }
@@ -664,13 +659,14 @@ void init_sgm_kernels() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    set_attrs<2>(optin); set_attrs<4>(optin); set_attrs<6>(optin);
-    set_attrs<8>(optin); set_attrs<12>(optin); set_attrs<16>(optin);
+    for (int dpl : kDplChoices) cudaFuncSetAttribute(kernel_for(dpl), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaGetLastError();
 }
 
 // Rows per band: enough bands to cover the image in one wave of persistent CTAs when it fits
 // (R = ceil(Hp / SMs)), else the largest band the block can hold; force_R overrides (tuning).
+// ngroups counts the work items of one launch (two passes x nbands), each with a progress counter and a
+// hand-off record row.
 SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands are never clustered*/) {
     SgmPlan p{};
     int optin = 227 * 1024, sms = 152;
@@ -678,13 +674,13 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();
     int rmax = g.dpl >= 12 ? kRowsMaxWide : kRowsMax;
-    while (rmax > 1 && sgm_smem(rmax, g.dp, 1).total > (size_t)optin) rmax--;
+    while (rmax > 1 && sgm_smem(rmax, g.dp).total > (size_t)optin) rmax--;
     int R = std::max(1, std::min(rmax, (g.Hp + sms - 1) / sms));
     if (force_R) R = std::max(1, std::min(rmax, force_R));
-    const void *fn = kernel_for(g.dpl, 1);
+    const void *fn = kernel_for(g.dpl);
     if (!fn) return p;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, g.dp, 1).total) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, g.dp).total) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -693,8 +689,8 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
     p.R = R;
     p.cs = 1;
     p.nbands = (g.Hp + R - 1) / R;
-    p.ngroups = p.nbands;
-    p.nclusters = std::min(p.nbands, per_sm * sms); // persistent CTAs, all co-resident
+    p.ngroups = 2 * p.nbands;
+    p.nclusters = std::min(p.ngroups, per_sm * sms); // persistent CTAs, all co-resident
     return p;
 }
 
@@ -702,20 +698,36 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
     return (size_t)std::max(p.ngroups, 1) * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
 }
 
-cudaError_t launch_sgm_pass(const Geom &g, const SgmPlan &p, SgmArgs a, int pass, cudaStream_t st) {
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
     a.R = p.R;
     a.cs = 1;
     a.nbands = p.nbands;
     a.ngroups = p.ngroups;
-    const void *fn = kernel_for(g.dpl, pass);
+    const void *fn = kernel_for(g.dpl);
     if (!fn) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.nbands * sizeof(unsigned), st);
+    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&a};
-    // cooperative launch: every CTA is resident, so a band never waits on a band that cannot run
+    // cooperative launch: every CTA is resident, and each work item depends only on work items of lower
+    // index (the previous band of its pass), so no item waits on one that cannot run
     return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R * 4 + kHelpers) * 32), args,
-                                       sgm_smem(p.R, g.dp, pass).total, st);
+                                       sgm_smem(p.R, g.dp).total, st);
+}
+
+cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *out, uint16_t *disp,
+                           cudaStream_t st) {
+    const unsigned blocks = (unsigned)((g.plane + 7) / 8);
+    switch (g.dpl) {
+    case 2: sgm_wta_kernel<2><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 4: sgm_wta_kernel<4><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 6: sgm_wta_kernel<6><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 8: sgm_wta_kernel<8><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 12: sgm_wta_kernel<12><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 16: sgm_wta_kernel<16><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 } // namespace sister

@@ -5,7 +5,7 @@
 // code running inside another framework that owns every device allocation, or a process that must not
 // touch the CUDA allocator after start-up. sister_aggregate_static serves them: it runs the 8-path
 // aggregation + winner-take-all of sister_compute on a cost volume the caller already holds, and keeps
-// all of its scratch (pass sum, hand-off records, progress counters, error flag) in one file-scope
+// all of its scratch (the two pass sums, hand-off records, progress counters, error flag) in one file-scope
 // device array of fixed size instead of calling cudaMalloc.
 #include "sister_gb300.h"
 #include "sister_internal.h"
@@ -90,7 +90,7 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     const size_t sum_bytes = align256(g.plane * g.dp * sizeof(uint16_t));
     const size_t bnd_bytes = align256(sgm_bnd_bytes(g, p));
     const size_t prog_bytes = align256((size_t)p.ngroups * sizeof(unsigned));
-    const size_t need = sum_bytes + bnd_bytes + prog_bytes + 256;
+    const size_t need = 2 * sum_bytes + bnd_bytes + prog_bytes + 256;
     if (need > kStaticScratchBytes) {
         char buf[256];
         std::snprintf(buf, sizeof buf,
@@ -102,11 +102,10 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     SgmArgs a{};
     a.cost = cost;
     a.sum0 = reinterpret_cast<uint16_t *>(b);
-    a.bnd = reinterpret_cast<uint16_t *>(b + sum_bytes);
-    a.progress = reinterpret_cast<unsigned *>(b + sum_bytes + bnd_bytes);
-    a.err = reinterpret_cast<unsigned *>(b + sum_bytes + bnd_bytes + prog_bytes);
-    a.out = out;
-    a.disp = disp_padded;
+    a.sum1 = reinterpret_cast<uint16_t *>(b + sum_bytes);
+    a.bnd = reinterpret_cast<uint16_t *>(b + 2 * sum_bytes);
+    a.progress = reinterpret_cast<unsigned *>(b + 2 * sum_bytes + bnd_bytes);
+    a.err = reinterpret_cast<unsigned *>(b + 2 * sum_bytes + bnd_bytes + prog_bytes);
     a.W = g.Wp;
     a.H = g.Hp;
     a.D = g.dc;
@@ -119,7 +118,8 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     // the arena keeps the previous call's contents: the error flag must start at zero (the progress
     // counters are cleared by each pass launch)
     cudaError_t e = cudaMemsetAsync(a.err, 0, sizeof(unsigned), st);
-    for (int pass = 0; pass < 2 && e == cudaSuccess; pass++) e = launch_sgm_pass(g, p, a, pass, st);
+    if (e == cudaSuccess) e = launch_sgm(g, p, a, st);
+    if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, out, disp_padded, st);
     unsigned flag = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, a.err, sizeof flag, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -61,7 +61,7 @@ struct sister_ctx {
     std::string err;
     bool loaded = false;
     int w = 0, h = 0, dc = 0;
-    DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, bnd, progress, errflag, disp, outs;
+    DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, sum1, bnd, progress, errflag, disp, outs;
     SgmPlan plan{};
     int plan_w = 0, plan_h = 0, plan_dc = 0;
     int tune_rows = 0, tune_cs = 0;
@@ -181,8 +181,9 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         {&c->med, 8 * plane * sizeof(uint16_t), "median"},
         {&c->masks, 4 * plane, "masks"},
         {&c->cost, vol * sizeof(uint16_t), "cost volume"},
-        {&c->sum0, vol * sizeof(uint16_t), "sum volume"},
-        {&c->bnd, sgm_bnd_bytes(g, p), "group boundary states"},
+        {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
+        {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
+        {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
         {&c->progress, (size_t)std::max(p.ngroups, 1) * sizeof(unsigned), "progress"},
         {&c->errflag, sizeof(unsigned), "error flag"},
         {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
@@ -231,11 +232,10 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         SgmArgs a{};
         a.cost = c->cost.as<uint16_t>();
         a.sum0 = c->sum0.as<uint16_t>();
+        a.sum1 = c->sum1.as<uint16_t>();
         a.bnd = c->bnd.as<uint16_t>();
         a.progress = c->progress.as<unsigned>();
         a.err = c->errflag.as<unsigned>();
-        a.out = dev_out[mode];
-        a.disp = c->disp.as<uint16_t>() + (size_t)mode * g.plane;
         a.W = g.Wp;
         a.H = g.Hp;
         a.D = g.dc;
@@ -244,12 +244,12 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.w = g.w;
         a.h = g.h;
         a.wait_limit_us = 2000000; // 2 s
-        e = launch_sgm_pass(g, plan, a, 0, st);
+        e = launch_sgm(g, plan, a, st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
-        c->mark(SISTER_STAGE_SGM0);
-        e = launch_sgm_pass(g, plan, a, 1, st);
-        if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
-        c->mark(SISTER_STAGE_SGM1);
+        c->mark(SISTER_STAGE_AGGREGATE);
+        e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode], c->disp.as<uint16_t>() + (size_t)mode * g.plane, st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
+        c->mark(SISTER_STAGE_WTA);
         c->last_mode = mode;
     }
     c->have_intermediates = true;
@@ -382,10 +382,13 @@ size_t sister_device_bytes(int width, int height, int dc) {
     const Geom g = make_geom(width, height, dc);
     if (g.dpl < 0) return 0;
     const size_t plane = g.plane, vol = plane * g.dp;
-    // group boundary records: at most one per band of one row (upper bound without a device query)
-    const size_t bnd = (size_t)g.Hp * g.Wp * (3 * (size_t)g.dp + 8) * 2;
-    return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 2 * vol * 2 +
-           bnd / 8 + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+    // band boundary records: one image row per band and pass, with the band height the launch plan picks on
+    // a 152-SM GB300 (the plan itself needs a device query), progress counters, sum volumes of both passes
+    const int R = std::max(1, std::min(g.dpl >= 12 ? 6 : 7, (g.Hp + 151) / 152));
+    const size_t nbands = (size_t)(g.Hp + R - 1) / R;
+    const size_t bnd = 2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2;
+    return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 3 * vol * 2 +
+           bnd + 2 * nbands * sizeof(unsigned) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
 }
 
 int sister_profile_enable(sister_ctx *c, int on) {

@@ -32,16 +32,15 @@ enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
 // Per-launch arguments of the aggregation (SGM) kernel.
 struct SgmArgs {
     const uint16_t *cost; // [Hp][Wp][dp] masked multiview cost
-    uint16_t *sum0;       // [Hp][Wp][dp] pass-0 path sum (written by pass 0, read by pass 1)
-    uint16_t *bnd;        // [nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row
-    unsigned *progress;   // [nbands] pixels of a band's last row published so far
+    uint16_t *sum0;       // [Hp][Wp][dp] 4-path sum of pass 0 (top-down)
+    uint16_t *sum1;       // [Hp][Wp][dp] 4-path sum of pass 1 (bottom-up)
+    uint16_t *bnd;        // [2][nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row, per pass
+    unsigned *progress;   // [2][nbands] pixels of a band's last row published so far, per pass
     unsigned *err;        // device error flag
-    uint16_t *out;        // [h][w] disparity*255 (pass 1), may be null
-    uint16_t *disp;       // [Hp][Wp] padded WTA disparity (pass 1), may be null
     int W, H, D, dp, dc, w, h;
-    int R;                // rows per band (4 path warps per row + fetcher + publisher per CTA)
+    int R;                // rows per band (4 path warps per row + fetcher, collector, writer per CTA)
     int cs;               // bands per group: always 1 (bands are not clustered)
-    int nbands, ngroups;
+    int nbands, ngroups;  // bands per pass; work items (2 * nbands)
     unsigned wait_limit_us; // longest wait of any warp (microseconds) before reporting kErrTimeout
 };
 
@@ -65,11 +64,14 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st);
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
-// Both aggregation passes plus the final WTA, crop and *255. Returns a cudaError_t.
+// Aggregation: both passes in one persistent launch (sums into sum0 / sum1), then the final WTA, crop and
+// *255 over the sum of the two. Return cudaError_t.
 // force_R: 0 = choose automatically; force_cs is accepted and ignored (groups are single bands)
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
-// one aggregation pass (0: top-down, stores the pass sum; 1: bottom-up, adds it and reduces)
-cudaError_t launch_sgm_pass(const Geom &g, const SgmPlan &p, SgmArgs a, int pass, cudaStream_t st);
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st);
+// out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
+cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *sum0, const uint16_t *sum1, uint16_t *out, uint16_t *disp,
+                           cudaStream_t st);
 
 } // namespace sister
