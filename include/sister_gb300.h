@@ -128,6 +128,30 @@ SISTER_API int sister_tune_set(sister_ctx *ctx, int key, int value);
 /* Read the value in effect for the current geometry (after set_max_disparity and load_views). */
 SISTER_API int sister_tune_get(sister_ctx *ctx, int key, int *value);
 
+/* --- batched rigs -------------------------------------------------------------------------------------
+ * Throughput path for many independent rigs (no reference counterpart: the reference computes one rig per
+ * SisterMultiviewDisparities object, hpp:18-26). Each rig is computed exactly as sister_compute would. */
+typedef struct sister_rig {
+    const uint8_t *views[5];   /* host images, reference constructor order: center, right, top, left, bottom */
+    int width, height, stride; /* stride in bytes */
+    int channels;              /* 1 (gray) or 3 (BGR) */
+    int max_disparity;         /* dispCount: multiple of 8 in [8, 512] */
+    uint16_t *multi, *horiz, *vert; /* host outputs, width*height u16 each (disparity*255); NULL skips a mode */
+} sister_rig;
+typedef struct sister_batch sister_batch;
+/* budget_bytes: device memory the engine may hold, allocated here as one arena (0: three quarters of the
+ * device's free memory). */
+SISTER_API int sister_batch_create(sister_batch **out, int device, size_t budget_bytes);
+SISTER_API void sister_batch_destroy(sister_batch *batch);
+SISTER_API const char *sister_batch_last_error(sister_batch *batch);
+/* Computes every rig and returns when all outputs are written. Rigs run in waves whose device memory fits
+ * the budget; within a wave the stages before the aggregation run per rig on several streams and one
+ * aggregation launch per disparity-stride class covers all of the wave's rigs. A rig that alone exceeds
+ * the budget fails the call with SISTER_EBUDGET (nothing of the call has run). */
+SISTER_API int sister_batch_run(sister_batch *batch, const sister_rig *rigs, int nrigs);
+/* Device bytes one rig takes inside a batch when nmodes of its outputs are requested. */
+SISTER_API size_t sister_batch_rig_bytes(int width, int height, int max_disparity, int nmodes);
+
 /* --- test hooks: intermediates of the last compute (device -> host copies) -------------------- */
 enum {
     SISTER_DBG_FRAMES = 1, /* index k=0..7: frame image k (u8) */

@@ -16,11 +16,12 @@ import os
 
 import numpy as np
 
-__all__ = ["SisterMultiviewDisparities", "Context", "SisterError", "load_library", "LIB_PATH"]
+__all__ = ["SisterMultiviewDisparities", "Context", "Batch", "SisterError", "load_library", "LIB_PATH"]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_gb300.so")
 
 SISTER_OK = 0
+SISTER_EINVAL, SISTER_ENOMEM, SISTER_EBUDGET, SISTER_EDEVICE, SISTER_ETIMEOUT, SISTER_ESTATE = -1, -2, -3, -4, -5, -6
 _ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
 
 STAGES = {1: "frames", 2: "census", 3: "pair_wta", 4: "median", 5: "masks", 6: "cost", 7: "aggregate", 8: "wta"}
@@ -38,6 +39,13 @@ _lib = None
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _u16p = ctypes.POINTER(ctypes.c_uint16)
 _vp = ctypes.c_void_p
+
+
+class SisterRig(ctypes.Structure):
+    """struct sister_rig of include/sister_gb300.h."""
+    _fields_ = [("views", ctypes.c_void_p * 5), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("stride", ctypes.c_int), ("channels", ctypes.c_int), ("max_disparity", ctypes.c_int),
+                ("multi", ctypes.c_void_p), ("horiz", ctypes.c_void_p), ("vert", ctypes.c_void_p)]
 
 
 def load_library(path: str | None = None) -> ctypes.CDLL:
@@ -69,6 +77,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                         ctypes.POINTER(ctypes.c_int)]
     lib.sister_tune_set.argtypes = [_vp, ctypes.c_int, ctypes.c_int]
     lib.sister_tune_get.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.sister_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_size_t]
+    lib.sister_batch_destroy.argtypes = [_vp]
+    lib.sister_batch_destroy.restype = None
+    lib.sister_batch_last_error.argtypes = [_vp]
+    lib.sister_batch_last_error.restype = ctypes.c_char_p
+    lib.sister_batch_run.argtypes = [_vp, ctypes.POINTER(SisterRig), ctypes.c_int]
+    lib.sister_batch_rig_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.sister_batch_rig_bytes.restype = ctypes.c_size_t
     if path is None:
         _lib = lib
     return lib
@@ -209,3 +225,58 @@ class SisterMultiviewDisparities:
     def compute_disparities(self, dispCount: int, multiview=True, horizontal=True, vertical=True):
         self.ctx.set_max_disparity(dispCount)
         return tuple(self.ctx.compute(multiview, horizontal, vertical))
+
+
+class Batch:
+    """Batched rigs (sister_batch): run(rigs) computes many rigs at once, bit-identical to Context.compute.
+
+    Each rig is (views, dispCount) or (views, dispCount, (multiview, horizontal, vertical)) with views in the
+    reference constructor order; run returns, per rig, the tuple of requested u16 h x w maps (None where a
+    mode was not requested)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.sister_batch_create(ctypes.byref(h), int(device), int(budget_bytes))
+        if rc != SISTER_OK:
+            raise SisterError(rc, "sister_batch_create(device=%d, budget=%d) failed" % (device, budget_bytes))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sister_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def rig_bytes(width: int, height: int, dc: int, nmodes: int = 1) -> int:
+        return int(load_library().sister_batch_rig_bytes(width, height, dc, nmodes))
+
+    def run(self, rigs):
+        arr = (SisterRig * len(rigs))()
+        keep, outs = [], []
+        for k, rig in enumerate(rigs):
+            views, dc = rig[0], rig[1]
+            modes = rig[2] if len(rig) > 2 else (True, False, False)
+            vs = _as_views(views)
+            keep.append(vs)
+            h, w = vs[0].shape[:2]
+            ch = 1 if vs[0].ndim == 2 else 3
+            r = arr[k]
+            for v in range(5):
+                r.views[v] = vs[v].ctypes.data
+            r.width, r.height, r.stride, r.channels, r.max_disparity = w, h, w * ch, ch, int(dc)
+            o = tuple(np.empty((h, w), np.uint16) if m else None for m in modes)
+            r.multi = o[0].ctypes.data if o[0] is not None else None
+            r.horiz = o[1].ctypes.data if o[1] is not None else None
+            r.vert = o[2].ctypes.data if o[2] is not None else None
+            outs.append(o)
+        rc = self.lib.sister_batch_run(self.h, arr, len(rigs))
+        if rc != SISTER_OK:
+            raise SisterError(rc, self.lib.sister_batch_last_error(self.h).decode(errors="replace"))
+        return outs

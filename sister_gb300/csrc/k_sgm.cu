@@ -165,7 +165,7 @@ constexpr unsigned kCheckEvery = 64; // blocking tests between looks at the erro
 // Bounded wait for the phase of parity `par`: after g.wait_limit_us microseconds, or once another warp has
 // raised the device error flag, the flag is raised and the caller proceeds (the host then reports
 // SISTER_ETIMEOUT), so no wait can hang the GPU.
-__device__ __forceinline__ void mbar_wait(uint32_t a, uint32_t par, const SgmArgs &g) {
+__device__ __forceinline__ void mbar_wait(uint32_t a, uint32_t par, const SgmLaunch &g) {
     if (mbar_test(a, par)) return;
     unsigned long long t0 = 0;
     for (unsigned n = 0;; n++) {
@@ -261,13 +261,14 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 // ---------------------------------------------------------------- the kernel
 template <int DPL>
 __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + kHelpers) * 32, 1)
-    sgm_kernel(const SgmArgs a) {
+    sgm_kernel(const SgmLaunch a) {
     constexpr int NP = DPL / 2;
     constexpr int KP = path_slots(32 * DPL), EB = KP / 2;
     constexpr int FB = batch_px(32 * DPL); // pixels per batched copy
     constexpr int KI = 2 * FB;             // incoming-ring slots (two batches)
     extern __shared__ __align__(128) unsigned char smem[];
-    const int R = a.R, W = a.W, H = a.H, dp = a.dp;
+    const int R = a.R, dp = a.dp;
+    int W = 0, H = 0; // geometry of the current work item's rig
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int d0 = lane * DPL;
     const int rec = rec_u16(dp), ps = pslot_u16(dp);
@@ -290,13 +291,8 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem + L.stage);
     uint16_t *cring = reinterpret_cast<uint16_t *>(smem + L.cring);
 
-    // halves holding disparities >= dc are infinite
-    uint32_t padm[NP];
-#pragma unroll
-    for (int k = 0; k < NP; k++)
-        padm[k] = ((d0 + 2 * k < a.D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < a.D) ? 0u : 0xFFFF0000u);
-
-    int pass = 0; // pass of the current work item: 0 top-down left-to-right, 1 mirrored
+    uint32_t padm[NP]; // halves holding disparities >= dc of the current rig are infinite
+    int pass = 0;      // pass of the current work item: 0 top-down left-to-right, 1 mirrored
     // A batch b of FB pixels (q = FB*b ...) covers nb = min(FB, W - FB*b) pixels; in memory (columns j)
     // they are contiguous, ascending in pass 0 and descending in pass 1. offset of pixel q in its batch:
     auto boff = [&](int q) {
@@ -313,21 +309,37 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
     auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : FB * (b - NPF + 1); };
     auto hend = [&](int b) { return min(W, hstart(b + 1)); };
     auto hbatch = [&](int x) { return x < FB ? (x < 2 ? 0 : 31 - __clz(x)) : x / FB + NPF - 1; };
-    const int nhb = hbatch(W - 1) + 1;
 
     const int role = wi / R; // 0: r0 + sum, 1..3: paths r1..r3, then fetcher, collector, writer
     const int w = wi % R;    // row within the band (compute warps)
-    const int nbat = (W + FB - 1) / FB;
     bool first_band = true;
-    for (int item = blockIdx.x; item < 2 * a.nbands; item += gridDim.x) {
-        pass = item & 1;
-        const int band = item >> 1;
-        uint16_t *sum = pass ? a.sum1 : a.sum0;
-        uint16_t *bnd = a.bnd + (size_t)pass * a.nbands * W * rec;
-        unsigned *progress = a.progress + (size_t)pass * a.nbands;
+    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        int band;
+        SgmRig rg;
+        if (a.items) {
+            const uint32_t v = a.items[item];
+            rg = a.rigs[v >> 24];
+            band = (int)((v >> 1) & 0x7FFFFFu);
+            pass = (int)(v & 1u);
+        } else {
+            rg = a.rig0;
+            band = item >> 1;
+            pass = item & 1;
+        }
+        W = rg.W;
+        H = rg.H;
+#pragma unroll
+        for (int k = 0; k < NP; k++)
+            padm[k] = ((d0 + 2 * k < rg.D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < rg.D) ? 0u : 0xFFFF0000u);
+        const int nhb = hbatch(W - 1) + 1;
+        const int nbat = (W + FB - 1) / FB;
+        const uint16_t *cost = rg.cost;
+        uint16_t *sum = pass ? rg.sum1 : rg.sum0;
+        uint16_t *bnd = rg.bnd + (size_t)pass * rg.nbands * W * rec;
+        unsigned *progress = rg.progress + (size_t)pass * rg.nbands;
         const int row0 = band * R;
         const int rows = min(R, H - row0);
-        const bool publish = rows == R && band + 1 < a.nbands;
+        const bool publish = rows == R && band + 1 < rg.nbands;
         if (threadIdx.x == 0) {
             if (!first_band)
                 for (int k = 0; k < L.nbar; k++) mbar_inval(bars + 8u * k);
@@ -370,7 +382,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                         const uint32_t bytes = (uint32_t)(bn(b) * dp * 2);
                         const size_t pix = rowbase + bj0(b);
                         mbar_expect_tx(cfull(w, b), bytes);
-                        bulk_g2s(sptr(myc + (size_t)(b & 1) * FB * dp), a.cost + pix * dp, bytes, cfull(w, b));
+                        bulk_g2s(sptr(myc + (size_t)(b & 1) * FB * dp), cost + pix * dp, bytes, cfull(w, b));
                     }
                 };
                 prefetch(0);
@@ -535,7 +547,7 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                     if (band == 0) {
                         const uint32_t bytes = (uint32_t)(nb * dp * 2);
                         mbar_expect_tx(infull(b), bytes);
-                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), a.cost + (rowbase0 + (pass ? W - he : hs)) * dp,
+                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), cost + (rowbase0 + (pass ? W - he : hs)) * dp,
                                  bytes, infull(b));
                         continue;
                     }
@@ -663,18 +675,26 @@ void init_sgm_kernels() {
     cudaGetLastError();
 }
 
+// largest band height whose shared-memory layout fits this device
+int sgm_rows_max(int dp, int device) {
+    int optin = 227 * 1024;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    cudaGetLastError();
+    int rmax = dp >= 384 ? kRowsMaxWide : kRowsMax;
+    while (rmax > 1 && sgm_smem(rmax, dp).total > (size_t)optin) rmax--;
+    return rmax;
+}
+
 // Rows per band: enough bands to cover the image in one wave of persistent CTAs when it fits
 // (R = ceil(Hp / SMs)), else the largest band the block can hold; force_R overrides (tuning).
 // ngroups counts the work items of one launch (two passes x nbands), each with a progress counter and a
 // hand-off record row.
 SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands are never clustered*/) {
     SgmPlan p{};
-    int optin = 227 * 1024, sms = 152;
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();
-    int rmax = g.dpl >= 12 ? kRowsMaxWide : kRowsMax;
-    while (rmax > 1 && sgm_smem(rmax, g.dp).total > (size_t)optin) rmax--;
+    const int rmax = sgm_rows_max(g.dp, device);
     int R = std::max(1, std::min(rmax, (g.Hp + sms - 1) / sms));
     if (force_R) R = std::max(1, std::min(rmax, force_R));
     const void *fn = kernel_for(g.dpl);
@@ -698,21 +718,56 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
     return (size_t)std::max(p.ngroups, 1) * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
 }
 
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st) {
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
-    a.R = p.R;
-    a.cs = 1;
-    a.nbands = p.nbands;
-    a.ngroups = p.ngroups;
     const void *fn = kernel_for(g.dpl);
     if (!fn) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(a.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
+    rig.W = g.Wp;
+    rig.H = g.Hp;
+    rig.D = g.dc;
+    rig.nbands = p.nbands;
+    SgmLaunch a{};
+    a.rig0 = rig;
+    a.rigs = nullptr;
+    a.items = nullptr;
+    a.nitems = p.ngroups;
+    a.R = p.R;
+    a.dp = g.dp;
+    a.err = err;
+    a.wait_limit_us = 2000000; // 2 s
+    cudaError_t e = cudaMemsetAsync(rig.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&a};
     // cooperative launch: every CTA is resident, and each work item depends only on work items of lower
     // index (the previous band of its pass), so no item waits on one that cannot run
     return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R * 4 + kHelpers) * 32), args,
                                        sgm_smem(p.R, g.dp).total, st);
+}
+
+cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
+                             unsigned *err, int device, cudaStream_t st) {
+    const int dpl = dp / 32;
+    const void *fn = kernel_for(dpl);
+    if (!fn || R < 1 || nitems < 1) return cudaErrorInvalidValue;
+    int sms = 152, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, dp).total) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return cudaErrorInvalidConfiguration;
+    }
+    SgmLaunch a{};
+    a.rigs = rigs_dev;
+    a.items = items_dev;
+    a.nitems = nitems;
+    a.R = R;
+    a.dp = dp;
+    a.err = err;
+    a.wait_limit_us = 2000000; // 2 s
+    void *args[] = {(void *)&a};
+    return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R * 4 + kHelpers) * 32), args,
+                                       sgm_smem(R, dp).total, st);
 }
 
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *out, uint16_t *disp,

@@ -99,29 +99,21 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
         return report(err, errlen, SISTER_EBUDGET, buf);
     }
     unsigned char *b = static_cast<unsigned char *>(base);
-    SgmArgs a{};
+    SgmRig a{};
     a.cost = cost;
     a.sum0 = reinterpret_cast<uint16_t *>(b);
     a.sum1 = reinterpret_cast<uint16_t *>(b + sum_bytes);
     a.bnd = reinterpret_cast<uint16_t *>(b + 2 * sum_bytes);
     a.progress = reinterpret_cast<unsigned *>(b + 2 * sum_bytes + bnd_bytes);
-    a.err = reinterpret_cast<unsigned *>(b + 2 * sum_bytes + bnd_bytes + prog_bytes);
-    a.W = g.Wp;
-    a.H = g.Hp;
-    a.D = g.dc;
-    a.dp = g.dp;
-    a.dc = g.dc;
-    a.w = g.w;
-    a.h = g.h;
-    a.wait_limit_us = 2000000; // 2 s
+    unsigned *errflag = reinterpret_cast<unsigned *>(b + 2 * sum_bytes + bnd_bytes + prog_bytes);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the arena keeps the previous call's contents: the error flag must start at zero (the progress
-    // counters are cleared by each pass launch)
-    cudaError_t e = cudaMemsetAsync(a.err, 0, sizeof(unsigned), st);
-    if (e == cudaSuccess) e = launch_sgm(g, p, a, st);
+    // counters are cleared by the aggregation launch)
+    cudaError_t e = cudaMemsetAsync(errflag, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess) e = launch_sgm(g, p, a, errflag, st);
     if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, out, disp_padded, st);
     unsigned flag = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, a.err, sizeof flag, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, errflag, sizeof flag, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         cudaGetLastError();

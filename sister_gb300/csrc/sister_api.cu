@@ -229,22 +229,13 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         if (!dev_out[mode]) continue;
         launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
         c->mark(SISTER_STAGE_COST);
-        SgmArgs a{};
+        SgmRig a{};
         a.cost = c->cost.as<uint16_t>();
         a.sum0 = c->sum0.as<uint16_t>();
         a.sum1 = c->sum1.as<uint16_t>();
         a.bnd = c->bnd.as<uint16_t>();
         a.progress = c->progress.as<unsigned>();
-        a.err = c->errflag.as<unsigned>();
-        a.W = g.Wp;
-        a.H = g.Hp;
-        a.D = g.dc;
-        a.dp = g.dp;
-        a.dc = g.dc;
-        a.w = g.w;
-        a.h = g.h;
-        a.wait_limit_us = 2000000; // 2 s
-        e = launch_sgm(g, plan, a, st);
+        e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->mark(SISTER_STAGE_AGGREGATE);
         e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode], c->disp.as<uint16_t>() + (size_t)mode * g.plane, st);

@@ -29,18 +29,27 @@ Geom make_geom(int w, int h, int dc);
 // Device-side error codes written by kernels with bounded waits.
 enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
 
-// Per-launch arguments of the aggregation (SGM) kernel.
-struct SgmArgs {
+// One rig's aggregation buffers (all device pointers).
+struct SgmRig {
     const uint16_t *cost; // [Hp][Wp][dp] masked multiview cost
     uint16_t *sum0;       // [Hp][Wp][dp] 4-path sum of pass 0 (top-down)
     uint16_t *sum1;       // [Hp][Wp][dp] 4-path sum of pass 1 (bottom-up)
     uint16_t *bnd;        // [2][nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row, per pass
-    unsigned *progress;   // [2][nbands] pixels of a band's last row published so far, per pass
-    unsigned *err;        // device error flag
-    int W, H, D, dp, dc, w, h;
-    int R;                // rows per band (4 path warps per row + fetcher, collector, writer per CTA)
-    int cs;               // bands per group: always 1 (bands are not clustered)
-    int nbands, ngroups;  // bands per pass; work items (2 * nbands)
+    unsigned *progress;   // [2][nbands] pixels of a band's last row published so far, per pass (zeroed first)
+    int W, H, D;          // padded width and height, max disparity dc
+    int nbands;           // bands per pass = ceil(H / R)
+};
+
+// Arguments of one aggregation launch: the work items of one or several rigs that share the d-stride dp
+// (same kernel instantiation) and the band height R.
+struct SgmLaunch {
+    SgmRig rig0;            // the rig of a single-rig launch (rigs == nullptr): item k = pass k & 1, band k >> 1
+    const SgmRig *rigs;     // device array of rigs (multi-rig launch), or nullptr
+    const uint32_t *items;  // device array, rig << 24 | band << 1 | pass, in an order where every item comes
+                            // after the previous band of its rig and pass (multi-rig launch), or nullptr
+    int nitems;
+    int R, dp;              // rows per band (4 path warps per row + fetcher, collector, writer per CTA); d-stride
+    unsigned *err;          // device error flag
     unsigned wait_limit_us; // longest wait of any warp (microseconds) before reporting kErrTimeout
 };
 
@@ -69,7 +78,13 @@ void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom
 // force_R: 0 = choose automatically; force_cs is accepted and ignored (groups are single bands)
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmArgs a, cudaStream_t st);
+// single rig: rig.nbands is filled from the plan; rig.progress is zeroed here
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st);
+// several rigs of one d-stride class: rigs / items in device memory (progress counters already zeroed); grid
+// = min(nitems, resident CTAs)
+int sgm_rows_max(int dp, int device);
+cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
+                             unsigned *err, int device, cudaStream_t st);
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *sum0, const uint16_t *sum1, uint16_t *out, uint16_t *disp,
                            cudaStream_t st);
