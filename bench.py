@@ -39,7 +39,7 @@ CONFIG = {
     "parallelism": "replicas (one rig per GPU per step, no collective)",
 }
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
-# kernels of ours launched per compute (frames, census, pair WTA, median, masks, cost, 2 aggregation passes)
+# kernels of ours launched per compute (frames, census, pair WTA, median, masks, cost, aggregation, final WTA)
 KERNELS_PER_COMPUTE = 8
 
 
@@ -143,6 +143,53 @@ def cpu_baseline_c2(views, dc):
     t = time.perf_counter() - t0
     return {"value": rig_units() / t, "unit": UNIT, "cores": port.num_threads(), "kind": "port",
             "sample": "one full 1920x1080/256 rig, mode 0, oracle C restatement (OpenMP), %.1f s" % t}
+
+
+def batched_leg(local):
+    """C3: 64 uneven rigs (synth.batch_shapes(64, seed=3), mode 0) through sister_batch_run against the same
+    rigs as 64 sequential plain calls (one context, load views + compute per rig); host arrays in and out
+    for both, bit-exact comparison of every output."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    import sister_gb300 as sg
+    from sister_gb300 import synth
+
+    shapes = synth.batch_shapes(64, seed=3)
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        rigs = list(ex.map(lambda k: synth.rig_for_shape(*shapes[k], seed=1000 + k), range(len(shapes))))
+    units = sum(w * h * dc for w, h, dc in shapes) / 1e9
+    free, _ = torch.cuda.mem_get_info(local)
+    budget = int(min(free - (48 << 30), 200 << 30))
+    batch = sg.Batch(local, budget)
+    brigs = [(views, dc, (True, False, False)) for (views, _), dc in rigs]
+    got = batch.run(brigs)  # warm-up
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        got = batch.run(brigs)
+        times.append(time.perf_counter() - t0)
+    batch.close()
+    t_batch = min(times)
+    ctx = sg.Context(local)
+    big = max(range(len(shapes)), key=lambda k: shapes[k][0] * shapes[k][1] * shapes[k][2])
+    ctx.load_views(rigs[big][0][0])
+    ctx.set_max_disparity(rigs[big][1])
+    ctx.compute(True, False, False)  # buffers sized for the largest rig before timing
+    match = True
+    t0 = time.perf_counter()
+    for k, ((views, _), dc) in enumerate(rigs):
+        ctx.load_views(views)
+        ctx.set_max_disparity(dc)
+        m = ctx.compute(True, False, False)[0]
+        match = match and bool(np.array_equal(m, got[k][0]))
+    t_plain = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": "64 uneven rigs: w~U[320,2448], h~U[240,2048] (x16), dc in {64,128,192,256} <= w/4, mode 0, "
+                        "seeds 1000..1063; host arrays in/out",
+            "rigs": len(shapes), "gpix_disp": units, "batched_value": units / t_batch, "batched_s": t_batch,
+            "plain_value": units / t_plain, "plain_s": t_plain, "ratio": t_plain / t_batch,
+            "budget_gb": budget / 2**30, "outputs_match": match, "unit": UNIT}
 
 
 def run_gb300(args):
@@ -253,6 +300,8 @@ def run_gb300(args):
             "stage_ms_mean": {k: sum(v) / len(v) for k, v in stage_ms.items()},
             "roofline": roof, "clocks": clk,
         }
+        if world == 1 and not args.no_batched:
+            line["batched"] = batched_leg(local)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_c2(views, dc)
         print(json.dumps(line), flush=True)
@@ -322,6 +371,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-rig batched-vs-plain leg")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
     if args.rig:

@@ -148,7 +148,38 @@ def _sensor_noise(rnd: _Rand, img: np.ndarray, sigma2x: int = 2) -> np.ndarray:
 
 def make_rig(w: int, h: int, dmin: int, dmax: int, seed: int, tiles: int = 10, bump: bool = False,
              sigma_blur: float = 1.5):
-    """Returns (views, disparity): views = [center, right, top, left, bottom] u8 h x w; disparity int."""
+    """Returns (views, disparity): views = [center, right, top, left, bottom] u8 h x w; disparity int.
+
+    Uses the library's C port of this generator (sister_synth_rig, byte-identical) when the library is
+    built, else the numpy definition below."""
+    native = _make_rig_native(w, h, dmin, dmax, seed, tiles, bump, sigma_blur)
+    if native is not None:
+        return native
+    return make_rig_numpy(w, h, dmin, dmax, seed, tiles, bump, sigma_blur)
+
+
+def _make_rig_native(w, h, dmin, dmax, seed, tiles, bump, sigma_blur):
+    try:
+        from sister_gb300 import load_library
+        lib = load_library()
+    except (ImportError, OSError):
+        return None
+    views = np.empty((5, h, w), np.uint8)
+    disp = np.empty((h, w), np.int32)
+    import ctypes
+    f = lib.sister_synth_rig
+    f.argtypes = [ctypes.c_int] * 4 + [ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    rc = f(w, h, dmin, dmax, seed, tiles, int(bool(bump)), int(round(sigma_blur * 10)), views.ctypes.data,
+           disp.ctypes.data)
+    if rc != 0:
+        raise ValueError("sister_synth_rig rejected (%d, %d, %d, %d, %r)" % (w, h, dmin, dmax, sigma_blur))
+    return [views[k].copy() for k in range(5)], disp.astype(np.int64)
+
+
+def make_rig_numpy(w: int, h: int, dmin: int, dmax: int, seed: int, tiles: int = 10, bump: bool = False,
+                   sigma_blur: float = 1.5):
+    """The generator's definition in numpy (slow for large rigs)."""
     rnd = _Rand(seed)
     disp = disparity_map(rnd, h, w, dmin, dmax, tiles, bump)
     center = _texture(rnd, h, w, sigma_blur)

@@ -62,6 +62,16 @@ def test_generator_is_deterministic():
     assert views_sha(a) == views_sha(b) != views_sha(c)
 
 
+@pytest.mark.parametrize("args", [(64, 48, 2, 12, 11, 3, False, 1.5), (96, 64, 2, 20, 9, 4, True, 0.8),
+                                  (200, 148, 4, 64, 21, 10, True, 1.5), (320, 240, 8, 60, 5, 6, False, 0.8)])
+def test_native_generator_is_byte_identical(args):
+    """sister_synth_rig (the library's C port of make_rig) gives the same bytes as the numpy definition."""
+    a_views, a_disp = synth._make_rig_native(*args)
+    b_views, b_disp = synth.make_rig_numpy(*args)
+    assert views_sha(a_views) == views_sha(b_views)
+    assert np.array_equal(a_disp, b_disp)
+
+
 def test_batch_shapes_follow_workload_rules():
     shapes = synth.batch_shapes(64, seed=3)
     assert len(shapes) == 64
