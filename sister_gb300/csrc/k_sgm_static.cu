@@ -85,7 +85,8 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     int rc = scratch_for_device(dev, &base, err, errlen);
     if (rc) return rc;
 
-    const SgmPlan p = sgm_plan(g, dev);
+    // tallest bands: the fewest hand-off records for the arena (the arena, not parallelism, is the constraint)
+    const SgmPlan p = sgm_plan(g, dev, 64);
     if (p.R < 1) return report(err, errlen, SISTER_EDEVICE, "no launch configuration fits the aggregation kernel");
     const size_t sum_bytes = align256(g.plane * g.dp * sizeof(uint16_t));
     const size_t bnd_bytes = align256(sgm_bnd_bytes(g, p));
