@@ -192,6 +192,62 @@ def batched_leg(local):
             "budget_gb": budget / 2**30, "outputs_match": match, "unit": UNIT}
 
 
+def served_leg(local, rates=(10.0, 25.0, 50.0), seconds=2.0):
+    """C4: Poisson arrivals of single-rig requests (mix: 50% 640x480/128, 35% 1920x1080/256, 15% 2448x2048/256)
+    into the serving loop with a 16 GB device budget; latency = submission to outputs in host memory."""
+    import numpy as np
+    import random
+    import sister_gb300 as sg
+    from sister_gb300 import synth
+
+    mix = synth.SERVE_MIX  # ((p, w, h, dc), ...)
+    pools = []
+    for ci, (_, w, h, dc) in enumerate(mix):
+        n = 4 if w * h < 1e6 else 2
+        pools.append([(synth.rig_for_shape(w, h, dc, seed=2000 + 10 * ci + k)[0][0], dc) for k in range(n)])
+    srv = sg.Server(local, 16 << 30)
+    # warm-up: one of each class
+    for ci in range(len(mix)):
+        srv.wait(srv.submit(pools[ci][0][0], mix[ci][3]))
+    out = {"workload": "Poisson arrivals, mix 50%% 640x480/128, 35%% 1920x1080/256, 15%% 2448x2048/256, mode 0, "
+                       "16 GB device budget, dynamic batching; %.0f s per rate" % seconds, "unit": "ms", "rates": []}
+    rnd = random.Random(7)
+    for rate in rates:
+        sched = []
+        t = 0.0
+        while True:
+            t += rnd.expovariate(rate)
+            if t > seconds:
+                break
+            u = rnd.random()
+            ci = 0 if u < mix[0][0] else (1 if u < mix[0][0] + mix[1][0] else 2)
+            sched.append((t, ci))
+        b0 = srv.stats()
+        tickets = []
+        t0 = time.perf_counter()
+        for (ta, ci) in sched:
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            views, dc = pools[ci][len(tickets) % len(pools[ci])]
+            tickets.append((srv.submit(views, dc), ci))
+        lat = [[], [], []]
+        for tk, ci in tickets:
+            lat[ci].append(srv.wait(tk, 120000)[1])
+        span = time.perf_counter() - t0
+        b1 = srv.stats()
+        allv = sorted(x for l in lat for x in l)
+        pct = lambda v, q: float(np.percentile(v, q)) if v else None
+        units = sum(mix[ci][1] * mix[ci][2] * mix[ci][3] for _, ci in sched) / 1e9
+        out["rates"].append({
+            "arrivals_per_s": rate, "requests": len(allv), "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+            "p50_1080p_ms": pct(lat[1], 50), "p99_1080p_ms": pct(lat[1], 99),
+            "p99_640x480_ms": pct(lat[0], 99), "p99_2448x2048_ms": pct(lat[2], 99),
+            "served_gpix_disp_per_s": units / span, "batches": b1["batches"] - b0["batches"]})
+    srv.close()
+    return out
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -302,6 +358,8 @@ def run_gb300(args):
         }
         if world == 1 and not args.no_batched:
             line["batched"] = batched_leg(local)
+        if world == 1 and not args.no_served:
+            line["served"] = served_leg(local)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_c2(views, dc)
         print(json.dumps(line), flush=True)
@@ -372,6 +430,7 @@ def main():
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-rig batched-vs-plain leg")
+    ap.add_argument("--no-served", action="store_true", help="skip the Poisson serving leg")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
     if args.rig:

@@ -152,6 +152,29 @@ SISTER_API int sister_batch_run(sister_batch *batch, const sister_rig *rigs, int
 /* Device bytes one rig takes inside a batch when nmodes of its outputs are requested. */
 SISTER_API size_t sister_batch_rig_bytes(int width, int height, int max_disparity, int nmodes);
 
+/* --- serving loop ------------------------------------------------------------------------------------
+ * Requests (one rig each: dispCount + five images -> disparity images, the request shape of the reference's
+ * ROS service recipe, ros/README.md:6-15) are submitted from any host thread; a worker thread drains the
+ * queue into dynamic batches that fit the budget (sister_batch_run), in arrival order. The rig's views and
+ * outputs must stay valid until sister_server_wait returns for its ticket. */
+typedef struct sister_server sister_server;
+SISTER_API int sister_server_create(sister_server **out, int device, size_t budget_bytes);
+SISTER_API void sister_server_destroy(sister_server *server); /* finishes queued requests first */
+SISTER_API const char *sister_server_last_error(sister_server *server);
+/* SISTER_EBUDGET if the rig alone exceeds the budget (nothing queued) */
+SISTER_API int sister_server_submit(sister_server *server, const sister_rig *rig, uint64_t *ticket);
+/* Blocks up to timeout_ms for the request; returns its status (SISTER_ETIMEOUT if still running) and its
+ * latency from submission to outputs in host memory. */
+SISTER_API int sister_server_wait(sister_server *server, uint64_t ticket, int timeout_ms, double *latency_ms);
+SISTER_API int sister_server_stats(sister_server *server, uint64_t *batches, uint64_t *rigs);
+
+/* --- synthetic workloads ------------------------------------------------------------------------------
+ * Seeded synthetic rig (no dataset ships with the reference): views = 5 x h x w u8 (center, right, top,
+ * left, bottom), disparity = h x w (may be NULL). Byte-identical to sister_gb300/synth.py make_rig;
+ * sigma_tenths 15 or 8 (texture blur). Host only. */
+SISTER_API int sister_synth_rig(int width, int height, int dmin, int dmax, long long seed, int tiles, int bump,
+                                int sigma_tenths, uint8_t *views, int32_t *disparity);
+
 /* --- test hooks: intermediates of the last compute (device -> host copies) -------------------- */
 enum {
     SISTER_DBG_FRAMES = 1, /* index k=0..7: frame image k (u8) */

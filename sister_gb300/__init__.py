@@ -16,7 +16,7 @@ import os
 
 import numpy as np
 
-__all__ = ["SisterMultiviewDisparities", "Context", "Batch", "SisterError", "load_library", "LIB_PATH"]
+__all__ = ["SisterMultiviewDisparities", "Context", "Batch", "Server", "SisterError", "load_library", "LIB_PATH"]
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_gb300.so")
 
@@ -85,6 +85,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.sister_batch_run.argtypes = [_vp, ctypes.POINTER(SisterRig), ctypes.c_int]
     lib.sister_batch_rig_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.sister_batch_rig_bytes.restype = ctypes.c_size_t
+    lib.sister_server_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_size_t]
+    lib.sister_server_destroy.argtypes = [_vp]
+    lib.sister_server_destroy.restype = None
+    lib.sister_server_last_error.argtypes = [_vp]
+    lib.sister_server_last_error.restype = ctypes.c_char_p
+    lib.sister_server_submit.argtypes = [_vp, ctypes.POINTER(SisterRig), ctypes.POINTER(ctypes.c_uint64)]
+    lib.sister_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.sister_server_stats.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     if path is None:
         _lib = lib
     return lib
@@ -280,3 +288,67 @@ class Batch:
         if rc != SISTER_OK:
             raise SisterError(rc, self.lib.sister_batch_last_error(self.h).decode(errors="replace"))
         return outs
+
+
+def _fill_rig(r, views, dc, modes):
+    vs = _as_views(views)
+    h, w = vs[0].shape[:2]
+    ch = 1 if vs[0].ndim == 2 else 3
+    for v in range(5):
+        r.views[v] = vs[v].ctypes.data
+    r.width, r.height, r.stride, r.channels, r.max_disparity = w, h, w * ch, ch, int(dc)
+    o = tuple(np.empty((h, w), np.uint16) if m else None for m in modes)
+    r.multi = o[0].ctypes.data if o[0] is not None else None
+    r.horiz = o[1].ctypes.data if o[1] is not None else None
+    r.vert = o[2].ctypes.data if o[2] is not None else None
+    return vs, o
+
+
+class Server:
+    """Serving loop (sister_server): submit(views, dispCount[, modes]) from any thread returns a ticket;
+    wait(ticket) returns (outputs, latency_ms). Requests are computed in dynamic batches within the budget."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 16 << 30):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.sister_server_create(ctypes.byref(h), int(device), int(budget_bytes))
+        if rc != SISTER_OK:
+            raise SisterError(rc, "sister_server_create(device=%d, budget=%d) failed" % (device, budget_bytes))
+        self.h = h
+        self._live = {}
+
+    def submit(self, views, dc, modes=(True, False, False)) -> int:
+        r = SisterRig()
+        vs, o = _fill_rig(r, views, dc, modes)
+        t = ctypes.c_uint64(0)
+        rc = self.lib.sister_server_submit(self.h, ctypes.byref(r), ctypes.byref(t))
+        if rc != SISTER_OK:
+            raise SisterError(rc, "sister_server_submit failed")
+        self._live[t.value] = (vs, o)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        lat = ctypes.c_double(0)
+        rc = self.lib.sister_server_wait(self.h, ticket, int(timeout_ms), ctypes.byref(lat))
+        if rc == SISTER_ETIMEOUT:
+            raise TimeoutError("request %d still running after %d ms" % (ticket, timeout_ms))
+        vs, o = self._live.pop(ticket)
+        if rc != SISTER_OK:
+            raise SisterError(rc, self.lib.sister_server_last_error(self.h).decode(errors="replace"))
+        return o, lat.value
+
+    def stats(self):
+        b, r = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self.lib.sister_server_stats(self.h, ctypes.byref(b), ctypes.byref(r))
+        return {"batches": b.value, "rigs": r.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sister_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

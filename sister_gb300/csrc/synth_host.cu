@@ -13,18 +13,8 @@ struct Rand {
     uint64_t seed;
     uint64_t stream = 0;
     explicit Rand(long long s) : seed((uint64_t)s & 0xFFFFFFFFull) {}
-    // splitmix64 counter hash of (seed, stream, index) for index = 1..n (synth.py _splitmix)
-    void u64(size_t n, std::vector<uint64_t> &out) {
-        stream++;
-        const uint64_t base = seed * 0x9E3779B97F4A7C15ull + stream * 0xD1B54A32D192ED03ull;
-        out.resize(n);
-        for (size_t i = 0; i < n; i++) {
-            uint64_t z = base + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
-            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-            out[i] = z ^ (z >> 31);
-        }
-    }
+    // n integers uniform in [lo, hi] from the splitmix64 counter hash of (seed, stream, index), index = 1..n
+    // (synth.py _splitmix / _Rand.ints)
     void ints(long long lo, long long hi, size_t n, std::vector<int64_t> &out) {
         stream++;
         const uint64_t base = seed * 0x9E3779B97F4A7C15ull + stream * 0xD1B54A32D192ED03ull;
