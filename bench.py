@@ -41,6 +41,10 @@ CONFIG = {
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # kernels of ours launched per compute (frames, census, pair WTA, median, masks, cost, aggregation, final WTA)
 KERNELS_PER_COMPUTE = 8
+# DRAM bytes per padded cell of one aggregation launch, measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.825 + 1.221 GB for 992*832*256 cells. It exceeds
+# the 8 algorithmic bytes per cell by the band hand-off records.
+TRAFFIC_BYTES_PER_CELL = (0.825024256e9 + 1.221127e9) / (992 * 832 * 256)
 
 
 def rig_units() -> float:
@@ -341,7 +345,10 @@ def run_gb300(args):
         avg = sum(sgm) / len(sgm)
         achieved = 8.0 * cells / (avg / 1e3) / 1e9
         roof = {"kernel": "sgm_kernel (8-path aggregation, both passes in one launch)", "bound": "hbm",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": TRAFFIC_BYTES_PER_CELL * cells,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of sgm_kernel<8> on a 480x320/256 "
+                                  "rig (2.05 GB for 211 M padded cells), scaled to this launch by the cell count",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": 8 * cells, "launch_ms": avg}
 
     if rank == 0:
