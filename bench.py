@@ -252,6 +252,40 @@ def served_leg(local, rates=(10.0, 25.0, 50.0), seconds=2.0):
     return out
 
 
+def stress_leg(local):
+    """C5: the 4096x3000 rig at max disparity 512 (synth.rig_c5), plain path, views resident in HBM."""
+    import torch
+    import sister_gb300 as sg
+    from sister_gb300 import synth
+
+    (views, _), dc = synth.rig_c5(5)
+    h, w = views[0].shape
+    need = sg.load_library().sister_device_bytes(w, h, dc)
+    free, _ = torch.cuda.mem_get_info(local)
+    if free < need + (4 << 30):
+        return {"skipped": "needs %.0f GB of device memory, %.0f GB free" % (need / 2**30, free / 2**30)}
+    dev = [torch.from_numpy(v).cuda() for v in views]
+    out = torch.empty((h, w), dtype=torch.int16, device="cuda")
+    ctx = sg.Context(local)
+    st = torch.cuda.Stream()
+    ctx.set_stream(st.cuda_stream)
+    ctx.load_views_device([t.data_ptr() for t in dev], w, h, w, 1)
+    ctx.set_max_disparity(dc)
+    ctx.compute_device(out.data_ptr())
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(2):
+        ctx.compute_device(out.data_ptr())
+    e1.record(st)
+    ctx.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    ctx.close()
+    units = w * h * dc / 1e9
+    return {"workload": "stress rig 4096x3000 u8, maxdisp 512, mode 0 (32 tiles, disparity 20-500)",
+            "value": units / (ms / 1e3), "unit": UNIT, "ms_per_rig": ms, "device_bytes": need}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -367,6 +401,8 @@ def run_gb300(args):
             line["batched"] = batched_leg(local)
         if world == 1 and not args.no_served:
             line["served"] = served_leg(local)
+        if world == 1 and not args.no_stress:
+            line["stress"] = stress_leg(local)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_c2(views, dc)
         print(json.dumps(line), flush=True)
@@ -438,6 +474,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-rig batched-vs-plain leg")
     ap.add_argument("--no-served", action="store_true", help="skip the Poisson serving leg")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 4096x3000/512 stress rig")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
     if args.rig:
