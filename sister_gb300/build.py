@@ -1,4 +1,5 @@
-"""Build libsister_gb300.so in-tree for sm_103a with nvcc (translation units compiled in parallel).
+"""Build libsister_gb300.so in-tree for sm_103a with nvcc (translation units compiled in parallel), and the
+headless CLI sister_compute_disp (host C++ over the library's C ABI).
 
     python -m sister_gb300.build [--force]
 """
@@ -15,6 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsister_gb300.so")
+CLI_SRC = os.path.join(CSRC, "cli")
+CLI = os.path.join(HERE, "sister_compute_disp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,7 +44,34 @@ def _flags(extra: list[str] | None = None) -> list[str]:
                    "-I", CSRC, "-I", os.path.join(ROOT, "include")] + (extra or [])
 
 
+def _cli_sources() -> list[str]:
+    return sorted(os.path.join(CLI_SRC, f) for f in os.listdir(CLI_SRC) if f.endswith((".cpp", ".h")))
+
+
+def build_cli(force: bool = False) -> str:
+    """sister_compute_disp, linked against the in-tree library (rpath $ORIGIN)."""
+    srcs = _cli_sources()
+    newest = max(os.path.getmtime(p) for p in srcs + [LIB, __file__, os.path.join(ROOT, "include", "sister_gb300.h")])
+    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= newest:
+        return CLI
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = CLI + ".tmp.%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", CLI_SRC] + \
+          [p for p in srcs if p.endswith(".cpp")] + ["-L", HERE, "-lsister_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s%s" % (p.stdout, p.stderr))
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    lib = build_lib(force, verbose, ptxas_info)
+    build_cli(force)
+    return lib
+
+
+def build_lib(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     srcs = sources()
