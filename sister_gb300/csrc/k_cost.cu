@@ -11,7 +11,10 @@ namespace {
 // d > b, else popcount(Cc[a][b] ^ Cn[a][b-d]). Mode 0 uses all frames, 1 frames {0,2}, 2 frames {1,3}.
 // The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
 // (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
-// One warp per pixel, lanes over d; 8 pixels of one row per CTA.
+// One warp per pixel, lanes over d (lane l holds d = l + 32k, k < DPL); 8 pixels of one row per CTA. The
+// frame loop is outside the d loop so that the DPL census loads of one frame are independent and issue
+// back to back (the transposed frames' words come from L2).
+template <int DPL>
 __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__restrict__ census,
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
                                                           uint16_t *__restrict__ cost) {
@@ -20,45 +23,46 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     if (j >= g.Wp) return;
     const size_t p = (size_t)i * g.Wp + j;
     const int D = g.dc;
-
-    bool use[4];
-    int fa[4], fb[4], fh[4], fw[4];
-    uint64_t cc[4];
-    const uint64_t *cn[4];
+    uint32_t acc[DPL];
+#pragma unroll
+    for (int k = 0; k < DPL; k++) acc[k] = 0;
 #pragma unroll
     for (int f = 0; f < 4; f++) {
         const bool in_mode = (mode == 0) || (mode == 1 && !(f & 1)) || (mode == 2 && (f & 1));
-        use[f] = in_mode && masks[(size_t)f * g.plane + p];
+        if (!in_mode || !masks[(size_t)f * g.plane + p]) continue; // warp-uniform
+        int fa, fb;
         switch (f) {
-        case 0: fa[f] = i; fb[f] = j; break;
-        case 2: fa[f] = i; fb[f] = g.Wp - 1 - j; break;
-        case 1: fa[f] = g.Wp - 1 - j; fb[f] = g.Hp - 1 - i; break;
-        default: fa[f] = g.Wp - 1 - j; fb[f] = i; break;
+        case 0: fa = i; fb = j; break;
+        case 2: fa = i; fb = g.Wp - 1 - j; break;
+        case 1: fa = g.Wp - 1 - j; fb = g.Hp - 1 - i; break;
+        default: fa = g.Wp - 1 - j; fb = i; break;
         }
-        fh[f] = g.frows(f);
-        fw[f] = g.fcols(f);
-        const uint64_t *base = census + (size_t)(2 * f) * g.plane + (size_t)fa[f] * fw[f];
-        cc[f] = use[f] ? base[fb[f]] : 0;
-        cn[f] = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa[f] * fw[f] + fb[f];
+        const int fh = g.frows(f), fw = g.fcols(f);
+        if (fa < 3 || fa >= fh - 2) { // whole frame row constant: 255 (rows 0..2) or 0 (never written)
+            const uint32_t c = fa < 3 ? 255u : 0u;
+#pragma unroll
+            for (int k = 0; k < DPL; k++) acc[k] += c;
+            continue;
+        }
+        const uint64_t cc = census[(size_t)(2 * f) * g.plane + (size_t)fa * fw + fb];
+        const uint64_t *cn = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa * fw + fb;
+        uint64_t wv[DPL];
+#pragma unroll
+        for (int k = 0; k < DPL; k++) {
+            const int d = lane + 32 * k;
+            wv[k] = (d <= fb && d < D) ? __ldg(cn - d) : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < DPL; k++) {
+            const int d = lane + 32 * k;
+            acc[k] += d > fb ? 255u : (uint32_t)__popcll(cc ^ wv[k]);
+        }
     }
     uint16_t *out = cost + p * g.dp;
-    for (int d = lane; d < g.dp; d += 32) {
-        uint32_t s = 0;
-        if (d >= D) {
-            s = 0x7FFFu;
-        } else {
 #pragma unroll
-            for (int f = 0; f < 4; f++) {
-                if (!use[f]) continue;
-                uint32_t c;
-                if (fa[f] < 3) c = 255;
-                else if (fa[f] >= fh[f] - 2) c = 0;
-                else if (d > fb[f]) c = 255;
-                else c = (uint32_t)__popcll(cc[f] ^ __ldg(cn[f] - d));
-                s += c;
-            }
-        }
-        out[d] = (uint16_t)s;
+    for (int k = 0; k < DPL; k++) {
+        const int d = lane + 32 * k;
+        out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
     }
 }
 
@@ -67,7 +71,14 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st) {
     dim3 grid((g.Wp + 7) / 8, g.Hp);
-    masked_cost_kernel<<<grid, 256, 0, st>>>(census, masks, g, mode, cost);
+    switch (g.dpl) {
+    case 2: masked_cost_kernel<2><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    case 4: masked_cost_kernel<4><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    case 6: masked_cost_kernel<6><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    case 8: masked_cost_kernel<8><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    case 12: masked_cost_kernel<12><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    default: masked_cost_kernel<16><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
+    }
 }
 
 } // namespace sister

@@ -10,27 +10,37 @@ namespace {
 // same keys key(a, b) = popc(Cc[a] ^ Cn[b]) << 16 | (a - b) over the band 0 <= a - b < D:
 //   L(a) = min over b of key(a, b)   (d = a - b <= min(a, D-1))
 //   R(b) = min over a of key(a, b)   (k = a - b <= min(D-1, W-1-b))
-// so every cell is counted once (POPC is the bound). A warp owns 32 consecutive columns b (one per lane)
-// and walks the diagonals d = 0..D-1: lane l meets cell (b0+l+d, b0+l), keeps R of its column in a
-// register, and carries the partial L of row a = b0+l+d, which moves one lane down per step; lane 0's
-// partial is then complete for this block and is merged into a shared array with atomicMin.
+// so every cell is counted once. A warp owns 32 consecutive columns b (one per lane) and walks the
+// diagonals d = 0..D-1, two per step: lane l keeps R of its column in a register and carries the partial L
+// of row a = b0+l+d, which moves down the lanes as d grows; rows whose cells in this block are all seen are
+// merged into a shared array with atomicMin.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
 // One CTA per frame row; both census rows staged in shared memory.
+// Two diagonals per step: lane l meets cells (b0+l+d, b0+l) and (b0+l+d+1, b0+l). Before the step lane l
+// carries the partial L of row a = b0+l+d; that row gets the first cell of lane l and the second cell of
+// lane l-1. After the step the rows of lanes 0 and 1 have no later cell in this block: they are merged and
+// the partials move two lanes down (lane 31's second cell starts the row that enters at lane 30). dmax is
+// even (D is a multiple of 8, W - b0 a multiple of 4).
 template <bool EDGE>
 __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b0, int lane, int W, int dmax,
                                           uint32_t *lk, uint32_t &racc) {
     uint32_t lacc = 0xFFFFFFFFu;
     const int b = b0 + lane;
-#pragma unroll 4
-    for (int d = 0; d < dmax; d++) {
+#pragma unroll 2
+    for (int d = 0; d < dmax; d += 2) {
         const int a = b + d;
-        uint32_t key = 0xFFFFFFFFu;
-        if (!EDGE || a < W) key = ((uint32_t)__popcll(cc[EDGE ? min(a, W - 1) : a] ^ cb) << 16) | (uint32_t)d;
-        racc = min(racc, key);
-        lacc = min(lacc, key);
-        if (lane == 0) atomicMin(&lk[b0 + d], lacc); // a = b0 + d: no later cell of this block
-        lacc = __shfl_down_sync(0xFFFFFFFFu, lacc, 1);
-        if (lane == 31) lacc = 0xFFFFFFFFu;
+        uint32_t k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu;
+        if (!EDGE || a < W) k0 = ((uint32_t)__popcll(cc[EDGE ? min(a, W - 1) : a] ^ cb) << 16) | (uint32_t)d;
+        if (!EDGE || a + 1 < W)
+            k1 = ((uint32_t)__popcll(cc[EDGE ? min(a + 1, W - 1) : a + 1] ^ cb) << 16) | (uint32_t)(d + 1);
+        racc = min(racc, min(k0, k1));
+        // second cell of lane l-1 (lane 0 receives lane 31's, whose row enters the warp at lane 30 below)
+        const uint32_t k1rot = __shfl_sync(0xFFFFFFFFu, k1, (lane + 31) & 31);
+        lacc = min(lacc, min(k0, lane == 0 ? 0xFFFFFFFFu : k1rot));
+        if (lane < 2) atomicMin(&lk[b0 + d + lane], lacc); // rows b0+d, b0+d+1: complete for this block
+        // move the partials two lanes down; lanes 30, 31 take lane 31's second cell and a fresh row
+        const uint32_t y = lane == 0 ? k1rot : (lane == 1 ? 0xFFFFFFFFu : lacc);
+        lacc = __shfl_sync(0xFFFFFFFFu, y, (lane + 2) & 31);
     }
     // lane l now carries row a = b0 + l + dmax, which may still have cells in later diagonals of other blocks
     if (b + dmax < W && lacc != 0xFFFFFFFFu) atomicMin(&lk[b + dmax], lacc);
@@ -83,24 +93,14 @@ __host__ __device__ inline int median_ring(int W) {
     return r;
 }
 
-__device__ __forceinline__ void cswap(uint32_t &a, uint32_t &b) {
-    const uint32_t t = min(a, b);
-    b = max(a, b);
-    a = t;
+__device__ __forceinline__ uint32_t med3(uint32_t a, uint32_t b, uint32_t c) { return max(min(a, b), min(max(a, b), c)); }
+__device__ __forceinline__ void sort3(uint32_t a, uint32_t b, uint32_t c, uint32_t &lo, uint32_t &mi, uint32_t &hi) {
+    const uint32_t l = min(a, b), h = max(a, b);
+    lo = min(l, c);
+    hi = max(h, c);
+    mi = max(l, min(h, c));
 }
-
-// Median of nine by the 19-exchange selection network; exact on integers.
-__device__ __forceinline__ uint32_t med9(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3, uint32_t v4, uint32_t v5,
-                                         uint32_t v6, uint32_t v7, uint32_t v8) {
-    cswap(v1, v2); cswap(v4, v5); cswap(v7, v8);
-    cswap(v0, v1); cswap(v3, v4); cswap(v6, v7);
-    cswap(v1, v2); cswap(v4, v5); cswap(v7, v8);
-    cswap(v0, v3); cswap(v5, v8); cswap(v4, v7);
-    cswap(v3, v6); cswap(v1, v4); cswap(v2, v5);
-    cswap(v4, v7); cswap(v4, v2); cswap(v6, v4);
-    cswap(v4, v2);
-    return v4;
-}
+constexpr int kMedRun = 4; // consecutive median positions per thread
 
 // median3x3_SSE(a, a, W, H) in place (postprocess.cpp:15-71 as called at SisterMultiviewDisparities.hpp:198
 // and siblings). Over the flattened array of N = W*H: out[x] = in[x] for x < W and x >= N-W-4;
@@ -158,11 +158,28 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
         asm volatile("cp.async.commit_group;" ::: "memory");
         const int e = min(s + per, end);
         const uint16_t *bi = bufs + (size_t)(c % (kMedPF + 1)) * blen - base(s); // bi[x] = in[x] for the span
-        for (int x = s + threadIdx.x; x < e; x += blockDim.x) {
-            const uint32_t v = med9(ring[(x - W - 1) & mask], ring[(x - W) & mask], ring[(x - W + 1) & mask],
-                                    bi[x - 1], bi[x], bi[x + 1], bi[x + W - 1], bi[x + W], bi[x + W + 1]);
-            ring[x & mask] = (uint16_t)v;
-            out[x] = (uint16_t)v;
+        // kMedRun consecutive positions per thread share their window columns: column c of position x's
+        // window is (out[c-W], in[c], in[c+W]) for c = x-1..x+1; each column is sorted once and the median
+        // of nine is med3(max of the column minima, med3 of the column medians, min of the column maxima).
+        // Columns past e are not needed (clamped to e: out[e-W] belongs to an earlier chunk).
+        for (int x0 = s + threadIdx.x * kMedRun; x0 < e; x0 += blockDim.x * kMedRun) {
+            uint32_t lo[kMedRun + 2], mi[kMedRun + 2], hi[kMedRun + 2];
+#pragma unroll
+            for (int k = 0; k < kMedRun + 2; k++) {
+                const int cx = min(x0 - 1 + k, e);
+                sort3(ring[(cx - W) & mask], bi[cx], bi[cx + W], lo[k], mi[k], hi[k]);
+            }
+#pragma unroll
+            for (int j = 0; j < kMedRun; j++) {
+                const int x = x0 + j;
+                if (x >= e) break;
+                const uint32_t l3 = max(lo[j], max(lo[j + 1], lo[j + 2]));
+                const uint32_t m3 = med3(mi[j], mi[j + 1], mi[j + 2]);
+                const uint32_t h3 = min(hi[j], min(hi[j + 1], hi[j + 2]));
+                const uint32_t v = med3(l3, m3, h3);
+                ring[x & mask] = (uint16_t)v;
+                out[x] = (uint16_t)v;
+            }
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -202,7 +219,9 @@ void init_mask_kernels() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncSetAttribute(pair_wta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    cudaFuncSetAttribute(median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, median_kernel); // its mbarriers are static shared memory
+    cudaFuncSetAttribute(median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
     cudaGetLastError();
 }
 
