@@ -47,9 +47,9 @@ __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b
 }
 
 __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
-                                                       uint16_t *__restrict__ wta) {
+                                                       uint16_t *__restrict__ wta, int f0) {
     extern __shared__ uint64_t srow[];
-    const int f = blockIdx.y;
+    const int f = f0 + blockIdx.y;
     const int H = g.frows(f), W = g.fcols(f), D = g.dc;
     const int i = blockIdx.x;
     if (i >= H) return;
@@ -112,9 +112,9 @@ constexpr int kMedRun = 4; // consecutive median positions per thread
 // kMedPF+1 buffers, so the sweep never waits on global memory and needs one CTA barrier per chunk.
 constexpr int kMedPF = 3;
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
-                                                      uint16_t *__restrict__ med) {
+                                                      uint16_t *__restrict__ med, int k0) {
     extern __shared__ __align__(16) uint16_t msm[];
-    const int k = blockIdx.x, f = k >> 1;
+    const int k = k0 + blockIdx.x, f = k >> 1;
     const int H = g.frows(f), W = g.fcols(f);
     const int N = W * H; // a multiple of 16 (W and H are multiples of 4)
     const uint16_t *in = wta + (size_t)k * g.plane;
@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) and the mask loops of SisterMultiviewDisparities.hpp:201-251:
 // keep = L <= j && |L - R[j-L]| <= 5; mask = keep && L > 0 && j >= dc; written in padded original
 // coordinates (frame 2: (i, Wp-1-j); frame 1: transpose + flip(-1); frame 3: transpose + flip(1)).
-__global__ void lrc_mask_kernel(const uint16_t *__restrict__ med, Geom g, uint8_t *__restrict__ masks) {
-    const int f = blockIdx.z;
+__global__ void lrc_mask_kernel(const uint16_t *__restrict__ med, Geom g, uint8_t *__restrict__ masks, int f0) {
+    const int f = f0 + blockIdx.z;
     const int H = g.frows(f), W = g.fcols(f);
     const int b = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
     if (a >= H || b >= W) return;
@@ -225,21 +225,21 @@ void init_mask_kernels() {
     cudaGetLastError();
 }
 
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st) {
+void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0, int nf) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
-    pair_wta_kernel<<<dim3(mx, 4), 256, smem, st>>>(census, g, wta);
+    pair_wta_kernel<<<dim3(mx, nf), 256, smem, st>>>(census, g, wta, f0);
 }
 
-void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st) {
+void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
-    median_kernel<<<8, 1024, smem, st>>>(wta, g, med);
+    median_kernel<<<2 * nf, 1024, smem, st>>>(wta, g, med, 2 * f0);
 }
 
-void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st) {
+void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    lrc_mask_kernel<<<dim3((mx + 255) / 256, mx, 4), 256, 0, st>>>(med, g, masks);
+    lrc_mask_kernel<<<dim3((mx + 255) / 256, mx, nf), 256, 0, st>>>(med, g, masks, f0);
 }
 
 } // namespace sister

@@ -68,9 +68,10 @@ void launch_to_gray(const uint8_t *const src[5], int stride, int channels, int w
                     cudaStream_t st);
 void launch_frames(const uint8_t *views_dev, const Geom &g, uint8_t *frames, cudaStream_t st);
 void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st);
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st);
-void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st);
-void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st);
+// the mask stages run on frames [f0, f0 + nf) (all four by default)
+void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4);
+void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4);
+void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
 // Aggregation: both passes in one persistent launch (sums into sum0 / sum1), then the final WTA, crop and
