@@ -14,27 +14,23 @@
 // on the wavefront above them, the other pass's bands keep the SMs busy.
 //
 // Work decomposition (one CTA = a band of R image rows, persistent over work items)
-//   * four "path warps" per row, one per path, each sweeping q = 0..W-1 with 32 lanes x DPL disparities.
-//     The row-to-row dependency chain (r3 trails the row above by one column) therefore costs one path
-//     update per hop instead of four;
-//   * the r0 warp of a row also owns the row's sum: it gathers r1, r2, r3 of each pixel from the other
-//     three warps, adds r0, and stores the pass's 4-path sum;
-//   * the r1, r2, r3 states of a row go to a KP-slot ring with one full barrier per slot (all three path
-//     warps arrive) and one empty barrier per slot (the row's r0 warp and the next row's three path warps
-//     arrive); producers check the empty barriers once per KP/2 pixels;
+//   * one warp per row sweeps q = 0..W-1 with 32 lanes x DPL disparities and updates all four paths of
+//     the pixel: r0 from its own registers, r1/r2/r3 from the row above. Column x of the row above is
+//     loaded once, at pixel x-1 (where r3 needs it), and its r2 and r1 states are kept in registers for
+//     the next two pixels. The four updates are independent, so they overlap; the warp adds them into the
+//     pass's sum itself. A row therefore trails the row above by about one pixel;
+//   * every row hands its new r1|r2|r3 states and their minima (one record per pixel) to the row below
+//     through a ring of kKP slots with a full and an empty barrier per slot; producers check the empty
+//     barriers once per half ring;
 //   * data from global memory arrives by bulk copies (TMA). A warp completes about one asynchronous copy
 //     per global-memory round trip however large it is (measured on GB300: ~500-750 cycles per copy for
 //     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows of FB
-//     consecutive pixels per copy into a two-group ring per row shared by the row's four warps, one group
-//     ahead;
-//   * the last row of a band is handed to the next band through global memory: a collector warp copies
-//     it into a staging ring (so the row never waits on global memory), a writer warp stores the records
-//     and, at the end of every hand-off batch (2, 2, 4 pixels, then FB at a time), fences and releases a
-//     progress counter. A fetcher warp of the next band polls that counter and bulk-copies each batch of
-//     records into a ring of 2*FB slots for its first row, so a band starts two pixels after the one above. In the
-//     first band the fetcher feeds the first line's cost rows to that line's path warps instead (they
-//     need no input), so the slow 8-bit-truncated r0 recurrence of the first line paces no other row.
-//     Compute warps never fence or poll global memory.
+//     consecutive pixels per copy into a two-group ring per row, one group ahead;
+//   * the last row of a band is handed to the next band through global memory: its ring (kKS slots) is
+//     read by a writer warp that stores the records and, at the end of every hand-off batch (2, 2, 4
+//     pixels, then FB at a time), fences and releases a progress counter. A fetcher warp of the next band
+//     polls that counter and bulk-copies each batch of records into a ring of 2*FB slots for its first
+//     row, so a band starts two pixels after the one above. Row warps never fence or poll global memory.
 // Arithmetic is packed u16x2: minima with __vminu2, additions and subtractions as plain 32-bit IADDs, which
 // equal packed u16x2 ones whenever no half carries or borrows. That holds on the recurrence: a path value is
 // C + (m - minLp) with minLp <= m <= minLp + 100, so real entries stay below 1021 + 100 and "infinite"
@@ -46,45 +42,42 @@
 #include "sister_internal.h"
 
 #include <algorithm>
+#include <vector>
 
 namespace sister {
 
-constexpr int kHelpers = 3;      // fetcher, collector, writer warps
-constexpr int kRowsMax = 7;      // rows per band for DPL <= 8: 4*7+3 = 31 warps
-constexpr int kRowsMaxWide = 6;  // rows per band for DPL >= 12: 27 warps (register file)
-constexpr int kKS = 8;           // staging-ring slots of the band's last row
-// pixels per batched copy: cost group of a row, and records (or first-line cost rows) per fetch
+constexpr int kHelpers = 2; // fetcher and writer warps
+constexpr int kKP = 4;      // ring slots of a row read by the row below
+constexpr int kKS = 8;      // ring slots of the band's last row, read by the writer
+// most rows per band (one warp each) by d-stride; shared memory may allow fewer
+__host__ __device__ constexpr int rows_cap(int dp) { return dp <= 256 ? 14 : dp <= 384 ? 12 : 9; }
+// pixels per batched copy: cost group of a row, and records per fetch
 __host__ __device__ constexpr int batch_px(int dp) { return dp >= 384 ? 4 : 8; }
-// path-ring slots (power of two; producers check the empty barriers every half ring)
-__host__ __device__ constexpr int path_slots(int dp) { return dp >= 384 ? 4 : 8; }
 
-// global hand-off record between bands: r1 | r2 | r3 (dp u16 each) | minima m1 m2 m3 (+5 pad)
+// one pixel's record, in ring slots and in the global hand-off rows alike: r1 | r2 | r3 (dp u16 each) |
+// minima m1 m2 m3 (+5 pad)
 __host__ __device__ inline int rec_u16(int dp) { return 3 * dp + 8; }
-// one path state in a ring slot: state (dp u16) | minimum (+7 pad)
-__host__ __device__ inline int pslot_u16(int dp) { return dp + 8; }
 
 struct SgmSmem {
-    size_t bars, prings, inring, stage, cring, total;
-    int nbar;
+    size_t bars, rings, inring, cring, total;
+    int nbar, nslot;
 };
-// barrier layout (8 bytes each; FB = batch_px(dp), KI = 2*FB, KP = path_slots(dp)):
-//   path ring of row w, slot s: full at 2*(w*KP + s), empty at +1
-//   incoming ring: batch full barriers [2] at in_base, per-slot empty barriers [KI] after them
-//   staging ring slot s: full at st_base + 2s, empty at +1;  cost group g (0, 1) of row w: c_base + 2w + g
+// ring slots: row w < R-1 owns slots [w*kKP, w*kKP + kKP), row R-1 owns [(R-1)*kKP, (R-1)*kKP + kKS)
+// barriers (8 bytes each; FB = batch_px(dp), KI = 2*FB): slot k full at 2k, empty at 2k+1; then the incoming
+// ring's batch full barriers [2] and per-slot empty barriers [KI]; then cost group g (0, 1) of row w at 2w + g
 __host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
     SgmSmem L{};
-    const int FB = batch_px(dp), KI = 2 * FB, KP = path_slots(dp);
-    L.nbar = R * KP * 2 + 2 + KI + kKS * 2 + R * 2;
+    const int FB = batch_px(dp), KI = 2 * FB;
+    L.nslot = (R - 1) * kKP + kKS;
+    L.nbar = 2 * L.nslot + 2 + KI + 2 * R;
     size_t o = 0;
     L.bars = o;
     o += (size_t)L.nbar * 8;
     o = (o + 127) & ~(size_t)127;
-    L.prings = o;
-    o += (size_t)R * KP * 3 * pslot_u16(dp) * 2;
+    L.rings = o;
+    o += (size_t)L.nslot * rec_u16(dp) * 2;
     L.inring = o;
     o += (size_t)KI * rec_u16(dp) * 2;
-    L.stage = o;
-    o += (size_t)kKS * rec_u16(dp) * 2;
     o = (o + 127) & ~(size_t)127;
     L.cring = o;
     o += (size_t)R * 2 * FB * dp * 2;
@@ -234,6 +227,10 @@ __device__ __forceinline__ uint32_t hmin(uint32_t v) { return min(v & 0xFFFFu, v
 
 // remaining-lines update of one path (sgm.cpp:278-383) for this lane's DPL = 2*NP disparities:
 //   L(d) = C(d) + min(Lp(d), Lp(d-1)+7, Lp(d+1)+7, minLp+100) - minLp; returns the lane's minimum
+// Per pair of disparities: one byte permute for the neighbours, min(Lp(d-1), Lp(d+1)) and min(Lp(d), minLp+100)
+// as packed minima, the +7 and the final minimum as one add-then-minimum, C + m - minLp as one 3-input add;
+// the lane minimum takes a 3-input packed minimum per two pairs. Every packed operation here is a single
+// instruction on sm_100+ (the add-then-minimum and 3-input minimum are DPX instructions).
 template <int NP>
 __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t minLp, const uint32_t (&C)[NP],
                                               uint32_t (&Ln)[NP], int lane) {
@@ -248,11 +245,13 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         const uint32_t x = perm_hi_lo(P[k], (k + 1 < NP) ? P[k + 1] : right); // (Lp[d+1], Lp[d+2])
-        const uint32_t t = __vminu2(xprev, x) + 0x00070007u;
-        const uint32_t m = __vminu2(t, __vminu2(P[k], p2));
+        const uint32_t m = __viaddmin_u16x2(__vminu2(xprev, x), 0x00070007u, __vminu2(P[k], p2));
         const uint32_t v = C[k] + m - m2;
         Ln[k] = v;
-        mn = __vminu2(mn, v);
+        if (k & 1)
+            mn = __vimin3_u16x2(mn, Ln[k - 1], v);
+        else if (k + 1 == NP)
+            mn = __vminu2(mn, v);
         xprev = x;
     }
     return hmin(mn);
@@ -260,58 +259,44 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
 
 // ---------------------------------------------------------------- the kernel
 template <int DPL>
-__global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + kHelpers) * 32, 1)
-    sgm_kernel(const SgmLaunch a) {
+__global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_kernel(const SgmLaunch a) {
     constexpr int NP = DPL / 2;
-    constexpr int KP = path_slots(32 * DPL), EB = KP / 2;
-    constexpr int FB = batch_px(32 * DPL); // pixels per batched copy
-    constexpr int KI = 2 * FB;             // incoming-ring slots (two batches)
+    constexpr int FB = batch_px(32 * DPL); // pixels per cost copy
+    constexpr int KI = 2 * FB;             // incoming-ring slots
     extern __shared__ __align__(128) unsigned char smem[];
     const int R = a.R, dp = a.dp;
     int W = 0, H = 0; // geometry of the current work item's rig
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int d0 = lane * DPL;
-    const int rec = rec_u16(dp), ps = pslot_u16(dp);
+    const int rec = rec_u16(dp);
     const SgmSmem L = sgm_smem(R, dp);
     const uint32_t bars = sptr(smem + L.bars);
-    auto pfull = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s); };
-    auto pempty = [&](int w, int s) { return bars + 16u * (uint32_t)(w * KP + s) + 8u; };
-    const uint32_t in_base = bars + 16u * (uint32_t)(R * KP);
+    // ring of row w: kKP slots (kKS for the last row); slot k's full barrier at bars + 16k, empty at +8
+    auto lgslots = [&](int w) { return w == R - 1 ? 3 : 2; };
+    const uint32_t in_base = bars + 16u * (uint32_t)L.nslot;
     auto infull = [&](int b) { return in_base + 8u * (uint32_t)(b & 1); };         // batch b
     auto inempty = [&](int x) { return in_base + 16u + 8u * (uint32_t)(x & (KI - 1)); }; // pixel x's slot
-    const uint32_t st_base = in_base + 16u + 8u * (uint32_t)KI;
-    auto sfull = [&](int s) { return st_base + 16u * (uint32_t)s; };
-    auto sempty = [&](int s) { return st_base + 16u * (uint32_t)s + 8u; };
-    const uint32_t c_base = st_base + 16u * (uint32_t)kKS;
+    const uint32_t c_base = in_base + 16u + 8u * (uint32_t)KI;
     auto cfull = [&](int w, int g) { return c_base + 8u * (uint32_t)(w * 2 + (g & 1)); };
-    uint16_t *prings = reinterpret_cast<uint16_t *>(smem + L.prings);
-    // state of path p (1..3) of row w in slot s
-    auto pslot = [&](int w, int p, int s) { return prings + (size_t)((w * KP + s) * 3 + (p - 1)) * ps; };
+    uint16_t *rings = reinterpret_cast<uint16_t *>(smem + L.rings);
     uint16_t *inring = reinterpret_cast<uint16_t *>(smem + L.inring);
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem + L.stage);
     uint16_t *cring = reinterpret_cast<uint16_t *>(smem + L.cring);
 
     uint32_t padm[NP]; // halves holding disparities >= dc of the current rig are infinite
     int pass = 0;      // pass of the current work item: 0 top-down left-to-right, 1 mirrored
-    // A batch b of FB pixels (q = FB*b ...) covers nb = min(FB, W - FB*b) pixels; in memory (columns j)
-    // they are contiguous, ascending in pass 0 and descending in pass 1. offset of pixel q in its batch:
-    auto boff = [&](int q) {
-        const int t = q % FB;
-        return pass ? (min(FB, W - (q - t)) - 1 - t) : t;
-    };
-    // first column (lowest j) of batch b, and its pixel count
+    // cost batch b of FB pixels (q = FB*b ...) covers min(FB, W - FB*b) pixels; in memory (columns j) they
+    // are contiguous, ascending in pass 0 and descending in pass 1. first column (lowest j) and pixel count:
     auto bj0 = [&](int b) { return pass ? max(0, W - FB * (b + 1)) : FB * b; };
     auto bn = [&](int b) { return min(FB, W - FB * b); };
-    // Hand-off batches of the incoming stream (previous band's records, or the first line's cost rows) start
-    // small so that a band can begin two pixels after the band above: pixels [0,2) [2,4) then doubling up to
-    // FB, then FB at a time (FB = 8: starts 0 2 4 8 16 24 ...). No batch wraps around the ring.
+    // Hand-off batches of the records of the band above start small so that a band can begin two pixels
+    // after the band above: pixels [0,2) [2,4) then doubling up to FB, then FB at a time (FB = 8: starts
+    // 0 2 4 8 16 24 ...). Each batch costs the writer a release and the fetcher a poll and a copy, so the
+    // batches are no smaller than the row's pixel period allows. No batch wraps around the ring.
     constexpr int NPF = (FB == 8) ? 3 : 2; // batches before the first full one
     auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : FB * (b - NPF + 1); };
     auto hend = [&](int b) { return min(W, hstart(b + 1)); };
     auto hbatch = [&](int x) { return x < FB ? (x < 2 ? 0 : 31 - __clz(x)) : x / FB + NPF - 1; };
 
-    const int role = wi / R; // 0: r0 + sum, 1..3: paths r1..r3, then fetcher, collector, writer
-    const int w = wi % R;    // row within the band (compute warps)
     bool first_band = true;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         int band;
@@ -336,222 +321,219 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
         const uint16_t *cost = rg.cost;
         uint16_t *sum = pass ? rg.sum1 : rg.sum0;
         uint16_t *bnd = rg.bnd + (size_t)pass * rg.nbands * W * rec;
-        unsigned *progress = rg.progress + (size_t)pass * rg.nbands;
+        unsigned *progress = rg.progress + (size_t)pass * rg.nbands * kProgressStride;
         const int row0 = band * R;
         const int rows = min(R, H - row0);
         const bool publish = rows == R && band + 1 < rg.nbands;
         if (threadIdx.x == 0) {
             if (!first_band)
                 for (int k = 0; k < L.nbar; k++) mbar_inval(bars + 8u * k);
-            for (int wr = 0; wr < R; wr++) {
-                // consumers of a row's slots: its r0 warp (32; not on the first line of the pass), plus the next
-                // row's three path warps (96) or, for the band's last row when another band follows, the
-                // collector (32)
-                const unsigned cons = ((row0 + wr == 0) ? 0u : 32u) +
-                                      ((wr + 1 < rows) ? 96u : (wr == R - 1 && publish) ? 32u : 0u);
-                for (int s = 0; s < KP; s++) {
-                    mbar_init(pfull(wr, s), 96);
-                    mbar_init(pempty(wr, s), cons > 0 ? cons : 1);
-                }
-                for (int g = 0; g < 2; g++) mbar_init(cfull(wr, g), 1); // r0's arrive.expect_tx + bytes
+            // ring slots: producer = the row's warp, consumer = the next row's warp or, for the last row, the
+            // writer (32 arrivals each)
+            for (int k = 0; k < L.nslot; k++) {
+                mbar_init(bars + 16u * k, 32);
+                mbar_init(bars + 16u * k + 8u, 32);
             }
+            for (int wr = 0; wr < R; wr++)
+                for (int g = 0; g < 2; g++) mbar_init(cfull(wr, g), 1); // row warp's arrive.expect_tx + bytes
             for (int b = 0; b < 2; b++) mbar_init(infull(b), 1);    // fetcher's arrive.expect_tx + bytes
-            for (int x = 0; x < KI; x++) mbar_init(inempty(x), 96); // the first row's r1, r2, r3 warps
-            for (int s = 0; s < kKS; s++) {
-                mbar_init(sfull(s), 32);  // collector
-                mbar_init(sempty(s), 32); // writer
-            }
+            for (int x = 0; x < KI; x++) mbar_init(inempty(x), 32); // the first row's warp
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
         first_band = false;
         __syncthreads();
 
-        if (role < 4 && w < rows) {
+        if (wi < rows) {
+            // ===================================================== row warp: all four paths of row w
+            // Record of pixel q in the row's ring: r3 and m3 are stored first and the full barrier of slot q
+            // is arrived on at once; r1, r2, m1, m2 follow in the same pixel and are covered by the next
+            // arrival (slot q+1; after the last pixel an arrival on the slot of a virtual pixel W). The row
+            // below needs r3 of column q+1 but r2 and r1 only of columns q and q-1, so it trails this row by
+            // one pixel plus the r3 update rather than by a whole pixel update. At its pixel p it reads r3 of
+            // column p+1 and r2, r1 of column p (r1 is kept in registers for pixel p+1) and releases column p.
+            const int w = wi;
             const int r = row0 + w;
             const int i = pass ? (H - 1 - r) : r;
             const bool first_line = (r == 0);
-            const size_t rowbase = (size_t)i * W;
+            const bool has_cons = (w + 1 < rows) || (w == R - 1 && publish);
+            const bool from_in = (w == 0); // the row above is the last row of the band above
+            const int lgs = lgslots(w), ns = 1 << lgs;
+            uint16_t *const oring = rings + (size_t)w * kKP * rec;
+            const uint32_t obar = bars + 16u * (uint32_t)(w * kKP);
+            const uint16_t *const aring = from_in ? inring : rings + (size_t)(w - 1) * kKP * rec;
+            const uint32_t abar = bars + 16u * (uint32_t)((w - 1) * kKP); // rows above the last: kKP slots
+            const int amask = from_in ? KI - 1 : kKP - 1;
             uint16_t *myc = cring + (size_t)w * 2 * FB * dp;
-            // position of pixel q in the row's cost ring: group (q/FB) & 1
-            auto cidx = [&](int q) { return (size_t)((((q / FB) & 1) * FB) + boff(q)) * dp; };
-            if (role == 0) {
-                // ================================================= r0 warp: cost prefetch, r0, sum
-                auto prefetch = [&](int b) {
-                    if (lane == 0 && b < nbat) {
-                        const uint32_t bytes = (uint32_t)(bn(b) * dp * 2);
-                        const size_t pix = rowbase + bj0(b);
-                        mbar_expect_tx(cfull(w, b), bytes);
-                        bulk_g2s(sptr(myc + (size_t)(b & 1) * FB * dp), cost + pix * dp, bytes, cfull(w, b));
-                    }
-                };
-                prefetch(0);
-                // r0 restarts every row from Lp = 0, minLp = 0 (sgm.cpp:215-216)
-                uint32_t r0[NP];
-                uint32_t r0min = 0;
-#pragma unroll
-                for (int k = 0; k < NP; k++) r0[k] = INF2 & padm[k];
-                for (int q = 0; q < W; q++) {
-                    if (q % FB == 0) {
-                        // group q/FB + 1 reuses the slots of group q/FB - 1, which every warp of the row has
-                        // finished: this warp gathered the path states of its last pixel (on the first line
-                        // this warp is the ring's only reader)
-                        prefetch(q / FB + 1);
-                        mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
-                    }
-                    const size_t ci = cidx(q);
-                    uint32_t c[NP];
-                    ldw<NP>(myc + ci + d0, c);
-                    uint32_t g[NP];
-                    if (first_line) {
-                        // First line (sgm.cpp:103-207): C' = (C == 255 ? 0 : C); r0 starts as C' and then runs the
-                        // recurrence in int32 truncated to 8 bits (saturate_cast<uint16>(uint8), types.h:28);
-                        // the sum receives r0 alone. r1..r3 of the first line only feed the row below.
-                        uint32_t cp[NP];
-#pragma unroll
-                        for (int k = 0; k < NP; k++) cp[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
-                        uint32_t mnv = 0xFFFFFFFFu;
-                        if (q == 0) {
-#pragma unroll
-                            for (int k = 0; k < NP; k++) {
-                                g[k] = cp[k];
-                                mnv = __vminu2(mnv, cp[k]);
-                            }
-                        } else {
-                            uint32_t tmp[NP];
-                            path_step<NP>(r0, r0min, cp, tmp, lane);
-#pragma unroll
-                            for (int k = 0; k < NP; k++) {
-                                g[k] = (tmp[k] & 0x00FF00FFu & ~padm[k]) | (INF2 & padm[k]);
-                                mnv = __vminu2(mnv, g[k]);
-                            }
-                        }
-#pragma unroll
-                        for (int k = 0; k < NP; k++) r0[k] = g[k];
-                        r0min = __reduce_min_sync(FULL, hmin(mnv));
-                    } else {
-                        uint32_t n0[NP];
-                        const uint32_t mn = path_step<NP>(r0, r0min, c, n0, lane);
-                        r0min = __reduce_min_sync(FULL, mn);
-                        const int s = q & (KP - 1);
-                        uint32_t v1[NP], v2[NP], v3[NP];
-                        mbar_wait(pfull(w, s), (q / KP) & 1, a);
-                        ldw<NP>(pslot(w, 1, s) + d0, v1);
-                        ldw<NP>(pslot(w, 2, s) + d0, v2);
-                        ldw<NP>(pslot(w, 3, s) + d0, v3);
-                        mbar_arrive(pempty(w, s));
-#pragma unroll
-                        for (int k = 0; k < NP; k++) {
-                            r0[k] = n0[k];
-                            g[k] = n0[k] + v1[k] + v2[k] + v3[k];
-                        }
-                    }
-                    // the pass's sum: first line r0 alone (sgm.cpp:132, :187), else r0+r1+r2+r3 (:386-391); u16
-                    // arithmetic never saturates or wraps for real disparities
-                    stw<NP>(sum + (rowbase + (pass ? (W - 1 - q) : q)) * dp + d0, g);
+            const size_t rowbase = (size_t)i * W;
+            auto prefetch = [&](int b) {
+                if (lane == 0 && b < nbat) {
+                    const uint32_t bytes = (uint32_t)(bn(b) * dp * 2);
+                    mbar_expect_tx(cfull(w, b), bytes);
+                    bulk_g2s(sptr(myc + (size_t)(b & 1) * FB * dp), cost + (rowbase + bj0(b)) * dp, bytes, cfull(w, b));
                 }
-                // every copy this warp issued has been waited for; after a timeout a wait may have returned
-                // early, so make sure none is still in flight before the barriers are reused
-                if (lane == 0)
-                    for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(cfull(w, b), (b / 2) & 1, a.wait_limit_us);
-            } else {
-                // ================================================= path warp p = role (1: r1, 2: r2, 3: r3)
-                const int p = role;
-                // input: the same path of the row above -- the ring of row w-1, or the incoming ring for w == 0
-                const bool from_in = (w == 0);
-                for (int q = 0; q < W; q++) {
-                    uint32_t c[NP];
-                    if (first_line) {
-                        // the first line's path warps take their cost rows from the fetcher's batches (incoming
-                        // ring, row of pixel q at position q % KI, batches stored in memory order), not from the
-                        // r0 warp's cost ring
-                        const int hb = hbatch(q), hs = hstart(hb), he = hend(hb);
-                        if (q == hs) mbar_wait(infull(hb), (hb / 2) & 1, a);
-                        ldw<NP>(inring + (size_t)(hs % KI + (pass ? he - 1 - q : q - hs)) * dp + d0, c);
-                        mbar_arrive(inempty(q));
-                    } else {
-                        if (q % FB == 0) mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
-                        ldw<NP>(myc + cidx(q) + d0, c);
+            };
+            // wait until column x of the row above is published up to its r3 (ring: r1 and r2 of x-1 too;
+            // incoming records are whole). Called for x = 1, 2, ..., W: the incoming ring is waited on at the
+            // first column of each batch and at x = 1, the first call (batch 0 holds columns 0 and 1).
+            auto wait_above = [&](int x) {
+                if (from_in) {
+                    const int hb = hbatch(x);
+                    if (x < W && (x == hstart(hb) || x == 1)) mbar_wait(infull(hb), (hb / 2) & 1, a);
+                } else {
+                    mbar_wait(abar + 16u * (uint32_t)(x & (kKP - 1)), (uint32_t)(x >> 2) & 1u, a);
+                }
+            };
+            auto release_above = [&](int x) {
+                mbar_arrive(from_in ? inempty(x) : abar + 16u * (uint32_t)(x & (kKP - 1)) + 8u);
+            };
+            prefetch(0);
+            // r0 restarts every row from Lp = 0, minLp = 0 (sgm.cpp:215-216)
+            uint32_t r0[NP];
+            uint32_t r0min = 0;
+#pragma unroll
+            for (int k = 0; k < NP; k++) r0[k] = INF2 & padm[k];
+            // r1 of column q-1 of the row above (column -1: outside the image, infinite with minimum 0)
+            uint32_t h1[NP];
+            uint32_t hm1 = 0;
+#pragma unroll
+            for (int k = 0; k < NP; k++) h1[k] = INF2;
+            uint16_t *sp = sum + (rowbase + (pass ? W - 1 : 0)) * dp + d0;
+            const ptrdiff_t sstep = pass ? -(ptrdiff_t)dp : (ptrdiff_t)dp;
+            const uint16_t *cg = myc;
+            int cn = 0;
+            for (int q = 0; q < W; q++) {
+                const int t = q % FB;
+                if (t == 0) {
+                    // group q/FB + 1 reuses the slots of group q/FB - 1, which this warp has finished
+                    prefetch(q / FB + 1);
+                    mbar_wait(cfull(w, q / FB), (q / FB / 2) & 1, a);
+                    cg = myc + (size_t)((q / FB) & 1) * FB * dp;
+                    cn = bn(q / FB);
+                }
+                uint32_t c[NP];
+                ldw<NP>(cg + (size_t)(pass ? cn - 1 - t : t) * dp + d0, c);
+                uint16_t *dst = oring + (size_t)(q & (ns - 1)) * rec;
+                const uint32_t ofull = obar + 16u * (uint32_t)(q & (ns - 1));
+                uint32_t n1[NP], n2[NP], n3[NP], g[NP];
+                uint32_t m1, m2, m3;
+                if (first_line) {
+                    // First line (sgm.cpp:103-207): C' = (C == 255 ? 0 : C); r0 starts as C' and then runs the
+                    // recurrence in int32 truncated to 8 bits (saturate_cast<uint16>(uint8), types.h:28);
+                    // the sum receives r0 alone. r1..r3 take C' with minimum min(C') (sgm.cpp:112-114,
+                    // :149-151, :192-194) and only feed the row below.
+                    uint32_t cmin = 0xFFFFFFFFu;
+#pragma unroll
+                    for (int k = 0; k < NP; k++) {
+                        n3[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
+                        cmin = __vminu2(cmin, n3[k]);
                     }
-                    uint32_t out[NP];
-                    uint32_t mn;
-                    if (first_line) {
-                        // first line: r1..r3 take C' with minimum min(C') (sgm.cpp:112-114, :149-151, :192-194)
-                        uint32_t mnv = 0xFFFFFFFFu;
+                    m3 = __reduce_min_sync(FULL, hmin(cmin));
+                    if (has_cons) {
+                        stw<NP>(dst + 2 * dp + d0, n3);
+                        if (lane == 0) dst[3 * dp + 2] = (uint16_t)m3;
+                        mbar_arrive(ofull);
+                    }
+                    uint32_t mnv = 0xFFFFFFFFu;
+                    if (q == 0) {
+#pragma unroll
+                        for (int k = 0; k < NP; k++) g[k] = n3[k];
+                        mnv = cmin;
+                    } else {
+                        uint32_t tmp[NP];
+                        path_step<NP>(r0, r0min, n3, tmp, lane);
 #pragma unroll
                         for (int k = 0; k < NP; k++) {
-                            out[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
-                            mnv = __vminu2(mnv, out[k]);
+                            g[k] = (tmp[k] & 0x00FF00FFu & ~padm[k]) | (INF2 & padm[k]);
+                            mnv = __vminu2(mnv, g[k]);
                         }
-                        mn = hmin(mnv);
-                    } else {
-                        // r3 reads column q+1 of the row above and never column 0: release that slot unread
-                        if (p == 3 && q == 0) mbar_arrive(from_in ? inempty(0) : pempty(w - 1, 0));
-                        // predecessor column: q-1 (r1), q (r2), q+1 (r3); outside the image: inf with min 0
-                        const int x = q + p - 2;
-                        uint32_t P[NP];
-                        uint32_t mp = 0;
-                        if (x >= 0 && x < W) {
-                            if (from_in) {
-                                // records arrive in batches; consumers take them in order, so a wait at the first
-                                // record of each batch (or the first one this warp reads) suffices
-                                const int hb = hbatch(x);
-                                if (x == hstart(hb) || x == (p == 3 ? 1 : 0)) mbar_wait(infull(hb), (hb / 2) & 1, a);
-                                const uint16_t *src = inring + (size_t)(x & (KI - 1)) * rec;
-                                ldw<NP>(src + (size_t)(p - 1) * dp + d0, P);
-                                mp = src[3 * dp + p - 1];
-                                mbar_arrive(inempty(x));
-                            } else {
-                                const int s = x & (KP - 1);
-                                mbar_wait(pfull(w - 1, s), (x / KP) & 1, a);
-                                const uint16_t *src = pslot(w - 1, p, s);
-                                ldw<NP>(src + d0, P);
-                                mp = src[dp];
-                                mbar_arrive(pempty(w - 1, s));
-                            }
-                        } else {
+                    }
 #pragma unroll
-                            for (int k = 0; k < NP; k++) P[k] = INF2;
-                        }
-                        mn = path_step<NP>(P, mp, c, out, lane);
+                    for (int k = 0; k < NP; k++) {
+                        r0[k] = g[k];
+                        n1[k] = n2[k] = n3[k];
                     }
-                    const uint32_t m = __reduce_min_sync(FULL, mn);
-                    // slots q .. q+EB-1 last held pixels q-KP .. q-KP+EB-1; every consumer releases in pixel
-                    // order, so the release of the last of them covers all
-                    if (q >= KP && (q & (EB - 1)) == 0) {
-                        const int y = q - KP + EB - 1;
-                        mbar_wait(pempty(w, y & (KP - 1)), (y / KP) & 1, a);
+                    r0min = __reduce_min_sync(FULL, hmin(mnv));
+                    m1 = m2 = m3;
+                } else {
+                    // r3 reads column q+1, r2 column q, r1 column q-1 of the row above (outside the image:
+                    // infinite states with minimum 0)
+                    wait_above(q + 1);
+                    uint32_t a2[NP], a3[NP];
+                    uint32_t am2, am3 = 0;
+                    if (q + 1 < W) {
+                        const uint16_t *s3 = aring + (size_t)((q + 1) & amask) * rec;
+                        ldw<NP>(s3 + 2 * dp + d0, a3);
+                        am3 = s3[3 * dp + 2];
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < NP; k++) a3[k] = INF2;
                     }
-                    const int s = q & (KP - 1);
-                    uint16_t *dst = pslot(w, p, s);
-                    stw<NP>(dst + d0, out);
-                    if (lane == 0) dst[dp] = (uint16_t)m;
-                    mbar_arrive(pfull(w, s));
+                    uint32_t b1[NP]; // r1 of column q, for pixel q+1
+                    uint32_t bm1;
+                    {
+                        const uint16_t *s2 = aring + (size_t)(q & amask) * rec;
+                        ldw<NP>(s2 + d0, b1);
+                        ldw<NP>(s2 + dp + d0, a2);
+                        const uint32_t mm = *reinterpret_cast<const uint32_t *>(s2 + 3 * dp);
+                        bm1 = mm & 0xFFFFu;
+                        am2 = mm >> 16;
+                        release_above(q);
+                    }
+                    // r3 first: the row below waits for it
+                    m3 = __reduce_min_sync(FULL, path_step<NP>(a3, am3, c, n3, lane));
+                    if (has_cons) {
+                        stw<NP>(dst + 2 * dp + d0, n3);
+                        if (lane == 0) dst[3 * dp + 2] = (uint16_t)m3;
+                        mbar_arrive(ofull);
+                    }
+                    uint32_t n0[NP];
+                    const uint32_t mn0 = path_step<NP>(r0, r0min, c, n0, lane);
+                    const uint32_t mn1 = path_step<NP>(h1, hm1, c, n1, lane);
+                    const uint32_t mn2 = path_step<NP>(a2, am2, c, n2, lane);
+                    r0min = __reduce_min_sync(FULL, mn0);
+                    m1 = __reduce_min_sync(FULL, mn1);
+                    m2 = __reduce_min_sync(FULL, mn2);
+#pragma unroll
+                    for (int k = 0; k < NP; k++) {
+                        r0[k] = n0[k];
+                        g[k] = n0[k] + n1[k] + n2[k] + n3[k];
+                        h1[k] = b1[k];
+                    }
+                    hm1 = bm1;
+                }
+                // the pass's sum: first line r0 alone (sgm.cpp:132, :187), else r0+r1+r2+r3 (:386-391); u16
+                // arithmetic never saturates or wraps for real disparities
+                stw<NP>(sp, g);
+                sp += sstep;
+                if (has_cons) {
+                    stw<NP>(dst + d0, n1);
+                    stw<NP>(dst + dp + d0, n2);
+                    if (lane == 0) *reinterpret_cast<uint32_t *>(dst + 3 * dp) = m1 | (m2 << 16);
+                    // the slot of pixel q+1 last held pixel q+1-ns (waited for here, off the r3 path)
+                    const int y = q + 1 - ns;
+                    if (y >= 0) mbar_wait(obar + 16u * (uint32_t)((q + 1) & (ns - 1)) + 8u, (uint32_t)(y >> lgs) & 1u, a);
                 }
             }
-        } else if (wi == 4 * R) {
-            // ===================================================== fetcher: batches of FB pixels -> inring
-            // band 0: the first line's cost rows; later bands: the previous band's last-row records
+            // virtual pixel W: publishes r1 and r2 of the last pixel
+            if (has_cons) mbar_arrive(obar + 16u * (uint32_t)(W & (ns - 1)));
+            // every copy this warp issued has been waited for; after a timeout a wait may have returned
+            // early, so make sure none is still in flight before the barriers are reused
+            if (lane == 0)
+                for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(cfull(w, b), (b / 2) & 1, a.wait_limit_us);
+        } else if (wi == R && band > 0) {
+            // ===================================================== fetcher: records of the band above -> inring
             if (lane == 0) {
-                const uint16_t *src = bnd + (size_t)(band > 0 ? band - 1 : 0) * W * rec;
-                const unsigned *prog = progress + (band > 0 ? band - 1 : 0);
-                const size_t rowbase0 = (size_t)(pass ? H - 1 : 0) * W;
+                const uint16_t *src = bnd + (size_t)(band - 1) * W * rec;
+                const unsigned *prog = progress + (size_t)(band - 1) * kProgressStride;
                 unsigned seen = 0;
                 for (int b = 0; b < nhb; b++) {
                     const int hs = hstart(b), he = hend(b), nb = he - hs;
-                    // before reusing barrier b & 1 every reader must be past batch b-2, and the ring slots of
-                    // pixels hs..he-1 must be free (they last held pixels hs-KI..he-1-KI); readers release in
-                    // pixel order, so waiting for the later of the two last pixels covers both
+                    // before reusing barrier b & 1 the reader must be past batch b-2, and the ring slots of
+                    // pixels hs..he-1 must be free (they last held pixels hs-KI..he-1-KI); the reader releases
+                    // in pixel order, so waiting for the later of the two last pixels covers both
                     const int y = max(b >= 2 ? hend(b - 2) - 1 : -1, he - 1 - KI);
                     if (y >= 0) mbar_wait(inempty(y), (y / KI) & 1, a);
-                    if (band == 0) {
-                        const uint32_t bytes = (uint32_t)(nb * dp * 2);
-                        mbar_expect_tx(infull(b), bytes);
-                        bulk_g2s(sptr(inring + (size_t)(hs % KI) * dp), cost + (rowbase0 + (pass ? W - he : hs)) * dp,
-                                 bytes, infull(b));
-                        continue;
-                    }
-                    uint16_t *dst = inring + (size_t)(hs % KI) * rec;
                     const unsigned need = (unsigned)he;
                     if (seen < need) {
                         const unsigned long long t0 = global_ns();
@@ -572,45 +554,28 @@ __global__ void __launch_bounds__((4 * (DPL >= 12 ? kRowsMaxWide : kRowsMax) + k
                     }
                     const uint32_t bytes = (uint32_t)(nb * rec * 2);
                     mbar_expect_tx(infull(b), bytes);
-                    bulk_g2s(sptr(dst), src + (size_t)hs * rec, bytes, infull(b));
+                    bulk_g2s(sptr(inring + (size_t)(hs % KI) * rec), src + (size_t)hs * rec, bytes, infull(b));
                 }
                 for (int b = max(0, nhb - 2); b < nhb; b++) mbar_drain(infull(b), (b / 2) & 1, a.wait_limit_us);
             }
-        } else if (wi == 4 * R + 1 && publish) {
-            // ===================================================== collector: band's last row -> staging ring
-            const int wl = R - 1;
-            for (int x = 0; x < W; x++) {
-                const int s = x & (kKS - 1);
-                if (x >= kKS) mbar_wait(sempty(s), ((x / kKS) - 1) & 1, a);
-                uint16_t *sd = stage + (size_t)s * rec;
-                const int ks = x & (KP - 1);
-                mbar_wait(pfull(wl, ks), (x / KP) & 1, a);
-                for (int p = 1; p <= 3; p++) {
-                    const uint16_t *sl = pslot(wl, p, ks);
-                    const uint4 *s4 = reinterpret_cast<const uint4 *>(sl);
-                    uint4 *d4 = reinterpret_cast<uint4 *>(sd + (size_t)(p - 1) * dp);
-                    for (int k = lane; k < dp / 8; k += 32) d4[k] = s4[k];
-                    if (lane == 0) sd[3 * dp + p - 1] = sl[dp];
-                }
-                mbar_arrive(pempty(wl, ks));
-                mbar_arrive(sfull(s));
-            }
-        } else if (wi == 4 * R + 2 && publish) {
-            // ===================================================== writer: staging ring -> global, progress
+        } else if (wi == R + 1 && publish) {
+            // ===================================================== writer: band's last row -> global, progress
+            // record x is complete once the last row has arrived on the slot of x+1 (x = W-1: virtual pixel W)
             uint16_t *dst = bnd + (size_t)band * W * rec;
+            const uint16_t *lring = rings + (size_t)(R - 1) * kKP * rec;
+            const uint32_t lbar = bars + 16u * (uint32_t)((R - 1) * kKP);
             const int nch = rec / 8; // 16-byte chunks per record
             for (int x = 0; x < W; x++) {
-                const int s = x & (kKS - 1);
-                mbar_wait(sfull(s), (x / kKS) & 1, a);
-                const uint4 *s4 = reinterpret_cast<const uint4 *>(stage + (size_t)s * rec);
+                mbar_wait(lbar + 16u * (uint32_t)((x + 1) & (kKS - 1)), (uint32_t)((x + 1) >> 3) & 1u, a);
+                const uint4 *s4 = reinterpret_cast<const uint4 *>(lring + (size_t)(x & (kKS - 1)) * rec);
                 uint4 *g4 = reinterpret_cast<uint4 *>(dst + (size_t)x * rec);
                 for (int k = lane; k < nch; k += 32) g4[k] = s4[k];
-                mbar_arrive(sempty(s));
+                mbar_arrive(lbar + 16u * (uint32_t)(x & (kKS - 1)) + 8u);
                 // releases at the end of every hand-off batch (the fetcher copies whole batches)
                 if (x + 1 == hend(hbatch(x))) {
                     __threadfence();
                     __syncwarp();
-                    if (lane == 0) st_release(progress + band, (unsigned)(x + 1));
+                    if (lane == 0) st_release(progress + (size_t)band * kProgressStride, (unsigned)(x + 1));
                 }
             }
         }
@@ -680,38 +645,90 @@ int sgm_rows_max(int dp, int device) {
     int optin = 227 * 1024;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     cudaGetLastError();
-    int rmax = dp >= 384 ? kRowsMaxWide : kRowsMax;
+    int rmax = rows_cap(dp);
     while (rmax > 1 && sgm_smem(rmax, dp).total > (size_t)optin) rmax--;
     return rmax;
 }
 
-// Rows per band: enough bands to cover the image in one wave of persistent CTAs when it fits
-// (R = ceil(Hp / SMs)), else the largest band the block can hold; force_R overrides (tuning).
-// ngroups counts the work items of one launch (two passes x nbands), each with a progress counter and a
-// hand-off record row.
-SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands are never clustered*/) {
+// largest band height on a GB300 (227 KB of shared memory per CTA), without a device query
+int sgm_rows_gb300(int dp) {
+    int rmax = rows_cap(dp);
+    while (rmax > 1 && sgm_smem(rmax, dp).total > 227 * 1024) rmax--;
+    return rmax;
+}
+
+namespace {
+// Rows per band. The plan simulates the persistent schedule: work item k (band k >> 1 of pass k & 1) runs on
+// CTA k mod (resident CTAs) after that CTA's previous item, and no earlier than one band lag after the
+// previous band of its pass; an item takes W pixel periods. A row warp's pixel period grows with the rows
+// its SM carries (issue slots are shared) above a latency floor, and the band lag is about one period per
+// row plus the hand-off (a batch of records and its release, poll and copy), so in units of one row's issue
+// time: period T = 20 + rows per SM, band lag = (1.2 R + 11) T. The band height with the earliest simulated
+// finish wins; ties go to the taller band (fewer hand-offs). per_sm(R): CTAs of band height R per SM.
+template <class F>
+SgmPlan plan_rows(const Geom &g, int sms, int lo, int hi, F per_sm) {
     SgmPlan p{};
+    double best = 0;
+    std::vector<double> free, start;
+    for (int R = hi; R >= lo; R--) {
+        const int k = per_sm(R);
+        if (k < 1) continue;
+        const int nb = (g.Hp + R - 1) / R;
+        const int items = 2 * nb;
+        const int conc = std::min(items, k * sms);
+        const double T = 20.0 + R * ((conc + sms - 1) / sms);
+        const double lag = (1.2 * R + 11.0) * T, sweep = (double)g.Wp * T;
+        free.assign(conc, 0.0);
+        start.assign(items, 0.0);
+        double end = 0;
+        for (int it = 0; it < items; it++) {
+            double s0 = free[it % conc];
+            if (it >= 2) s0 = std::max(s0, start[it - 2] + lag);
+            start[it] = s0;
+            free[it % conc] = s0 + sweep;
+            end = std::max(end, s0 + sweep);
+        }
+        if (p.R == 0 || end < best) {
+            best = end;
+            p.R = R;
+            p.nbands = nb;
+            p.ngroups = items;
+            p.nclusters = conc; // persistent CTAs, all co-resident
+        }
+    }
+    p.cs = p.R ? 1 : 0;
+    return p;
+}
+} // namespace
+
+// Launch plan on `device`; force_R fixes the band height (tuning). ngroups counts the work items of one
+// launch (two passes x nbands), each with a progress counter and a hand-off record row.
+SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands are never clustered*/) {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();
-    const int rmax = sgm_rows_max(g.dp, device);
-    int R = std::max(1, std::min(rmax, (g.Hp + sms - 1) / sms));
-    if (force_R) R = std::max(1, std::min(rmax, force_R));
     const void *fn = kernel_for(g.dpl);
-    if (!fn) return p;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, g.dp).total) !=
-            cudaSuccess ||
-        per_sm < 1) {
-        cudaGetLastError();
-        return p;
-    }
-    p.R = R;
-    p.cs = 1;
-    p.nbands = (g.Hp + R - 1) / R;
-    p.ngroups = 2 * p.nbands;
-    p.nclusters = std::min(p.ngroups, per_sm * sms); // persistent CTAs, all co-resident
-    return p;
+    if (!fn) return SgmPlan{};
+    const int rmax = sgm_rows_max(g.dp, device);
+    const int lo = force_R ? std::max(1, std::min(rmax, force_R)) : 1;
+    return plan_rows(g, sms, lo, force_R ? lo : rmax, [&](int R) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, fn, (R + kHelpers) * 32, sgm_smem(R, g.dp).total) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            k = 0;
+        }
+        return k;
+    });
+}
+
+// The same plan for a 152-SM GB300 without a device query (227 KB of shared memory per CTA, 228 KB and 64
+// warps per SM): used for memory estimates.
+SgmPlan sgm_plan_gb300(const Geom &g) {
+    if (!kernel_for(g.dpl)) return SgmPlan{};
+    return plan_rows(g, 152, 1, sgm_rows_gb300(g.dp), [&](int R) {
+        return (int)std::min<size_t>(228 * 1024 / (sgm_smem(R, g.dp).total + 1024), 64 / (R + kHelpers));
+    });
 }
 
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
@@ -735,12 +752,12 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
     a.dp = g.dp;
     a.err = err;
     a.wait_limit_us = 2000000; // 2 s
-    cudaError_t e = cudaMemsetAsync(rig.progress, 0, (size_t)p.ngroups * sizeof(unsigned), st);
+    cudaError_t e = cudaMemsetAsync(rig.progress, 0, progress_bytes(p.ngroups), st);
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&a};
     // cooperative launch: every CTA is resident, and each work item depends only on work items of lower
     // index (the previous band of its pass), so no item waits on one that cannot run
-    return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R * 4 + kHelpers) * 32), args,
+    return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R + kHelpers) * 32), args,
                                        sgm_smem(p.R, g.dp).total, st);
 }
 
@@ -751,7 +768,7 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
     if (!fn || R < 1 || nitems < 1) return cudaErrorInvalidValue;
     int sms = 152, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (4 * R + kHelpers) * 32, sgm_smem(R, dp).total) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (R + kHelpers) * 32, sgm_smem(R, dp).total) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -766,7 +783,7 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
     a.err = err;
     a.wait_limit_us = 2000000; // 2 s
     void *args[] = {(void *)&a};
-    return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R * 4 + kHelpers) * 32), args,
+    return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R + kHelpers) * 32), args,
                                        sgm_smem(R, dp).total, st);
 }
 

@@ -188,7 +188,7 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
         {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
         {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
-        {&c->progress, (size_t)std::max(p.ngroups, 1) * sizeof(unsigned), "progress"},
+        {&c->progress, progress_bytes(std::max(p.ngroups, 1)), "progress"},
         {&c->errflag, sizeof(unsigned), "error flag"},
         {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
         {&c->outs, 3 * (size_t)g.w * g.h * sizeof(uint16_t), "outputs"},
@@ -405,12 +405,23 @@ size_t sister_device_bytes(int width, int height, int dc) {
     if (g.dpl < 0) return 0;
     const size_t plane = g.plane, vol = plane * g.dp;
     // band boundary records: one image row per band and pass, with the band height the launch plan picks on
-    // a 152-SM GB300 (the plan itself needs a device query), progress counters, sum volumes of both passes
-    const int R = std::max(1, std::min(g.dpl >= 12 ? 6 : 7, (g.Hp + 151) / 152));
-    const size_t nbands = (size_t)(g.Hp + R - 1) / R;
+    // the current device (or a 152-SM GB300 when there is none), progress counters, sum volumes of both passes
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = -1;
+    }
+    SgmPlan p{};
+    if (dev >= 0) {
+        init_sgm_kernels();
+        p = sgm_plan(g, dev);
+    }
+    if (p.R < 1) p = sgm_plan_gb300(g);
+    if (p.R < 1) return 0;
+    const size_t nbands = (size_t)p.nbands;
     const size_t bnd = 2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2;
     return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 3 * vol * 2 +
-           bnd + 2 * nbands * sizeof(unsigned) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+           bnd + progress_bytes(2 * nbands) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
 }
 
 int sister_profile_enable(sister_ctx *c, int on) {

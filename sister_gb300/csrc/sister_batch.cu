@@ -43,7 +43,7 @@ RigBytes rig_bytes(int w, int h, int dc, int channels, int R) {
              al(8 * plane * 8) + 2 * al(8 * plane * 2) + al(4 * plane);
     const size_t nbands = (size_t)(g.Hp + R - 1) / R;
     const size_t vol = plane * g.dp * 2;
-    b.per_mode = 3 * al(vol) + al(2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2) + al(2 * nbands * 4) +
+    b.per_mode = 3 * al(vol) + al(2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2) + al(progress_bytes(2 * nbands)) +
                  al((size_t)w * h * 2);
     return b;
 }
@@ -166,11 +166,11 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
             j.sum0 = b->take<uint16_t>(vol);
             j.sum1 = b->take<uint16_t>(vol);
             j.bnd = b->take<uint16_t>(2 * (size_t)j.nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2);
-            j.progress = b->take<unsigned>(2 * (size_t)j.nbands * 4);
+            j.progress = b->take<unsigned>(progress_bytes(2 * (size_t)j.nbands));
             j.out = b->take<uint16_t>((size_t)w * h * 2);
             j.host_out = outs[mode];
             launch_masked_cost(census, masks, g, mode, j.cost, st);
-            e = cudaMemsetAsync(j.progress, 0, 2 * (size_t)j.nbands * sizeof(unsigned), st);
+            e = cudaMemsetAsync(j.progress, 0, progress_bytes(2 * (size_t)j.nbands), st);
             if (e != cudaSuccess) return b->cuda_fail(e, "reset progress");
             jobs.push_back(j);
         }
@@ -259,7 +259,7 @@ size_t sister_batch_rig_bytes(int width, int height, int max_disparity, int nmod
         cudaGetLastError();
         dev = -1;
     }
-    const int R = dev >= 0 ? sgm_rows_max(g.dp, dev) : (g.dpl >= 12 ? 6 : 7);
+    const int R = dev >= 0 ? sgm_rows_max(g.dp, dev) : sgm_rows_gb300(g.dp);
     const RigBytes rb = rig_bytes(width, height, max_disparity, 3, R);
     return rb.prep + (size_t)nmodes * rb.per_mode;
 }

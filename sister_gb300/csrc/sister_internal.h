@@ -26,6 +26,11 @@ constexpr int kDplChoices[] = {2, 4, 6, 8, 12, 16};
 int choose_dpl(int dc);
 Geom make_geom(int w, int h, int dc);
 
+// Band hand-off progress counters sit one per 128-byte line: the next band polls its counter from another SM
+// while the writer updates it, and neighbouring bands' counters must not share the line.
+constexpr int kProgressStride = 32;
+inline size_t progress_bytes(size_t ncounters) { return ncounters * kProgressStride * sizeof(unsigned); }
+
 // Device-side error codes written by kernels with bounded waits.
 enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
 
@@ -35,7 +40,8 @@ struct SgmRig {
     uint16_t *sum0;       // [Hp][Wp][dp] 4-path sum of pass 0 (top-down)
     uint16_t *sum1;       // [Hp][Wp][dp] 4-path sum of pass 1 (bottom-up)
     uint16_t *bnd;        // [2][nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row, per pass
-    unsigned *progress;   // [2][nbands] pixels of a band's last row published so far, per pass (zeroed first)
+    unsigned *progress;   // [2][nbands] x kProgressStride: pixels of a band's last row published so far, per
+                          // pass, one counter per 128-byte line (zeroed first)
     int W, H, D;          // padded width and height, max disparity dc
     int nbands;           // bands per pass = ceil(H / R)
 };
@@ -48,7 +54,7 @@ struct SgmLaunch {
     const uint32_t *items;  // device array, rig << 24 | band << 1 | pass, in an order where every item comes
                             // after the previous band of its rig and pass (multi-rig launch), or nullptr
     int nitems;
-    int R, dp;              // rows per band (4 path warps per row + fetcher, collector, writer per CTA); d-stride
+    int R, dp;              // rows per band (one warp per row + fetcher and writer per CTA); d-stride
     unsigned *err;          // device error flag
     unsigned wait_limit_us; // longest wait of any warp (microseconds) before reporting kErrTimeout
 };
@@ -78,12 +84,14 @@ void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom
 // *255 over the sum of the two. Return cudaError_t.
 // force_R: 0 = choose automatically; force_cs is accepted and ignored (groups are single bands)
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
+SgmPlan sgm_plan_gb300(const Geom &g); // the plan on a 152-SM GB300, without a device query
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
 // single rig: rig.nbands is filled from the plan; rig.progress is zeroed here
 cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st);
 // several rigs of one d-stride class: rigs / items in device memory (progress counters already zeroed); grid
 // = min(nitems, resident CTAs)
 int sgm_rows_max(int dp, int device);
+int sgm_rows_gb300(int dp); // sgm_rows_max on a GB300, without a device query
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
                              unsigned *err, int device, cudaStream_t st);
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
