@@ -39,8 +39,9 @@ CONFIG = {
     "parallelism": "replicas (one rig per GPU per step, no collective)",
 }
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
-# kernels of ours launched per compute (frames, census, pair WTA, median, masks, cost, aggregation, final WTA)
-KERNELS_PER_COMPUTE = 8
+# kernels of ours launched per compute: frames, census, pair WTA (one per frame orientation, 4), median (4),
+# masks (4), cost, aggregation (both passes), final WTA
+KERNELS_PER_COMPUTE = 17
 # DRAM bytes per padded cell of one aggregation launch, measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.825 + 1.221 GB for 992*832*256 cells. It exceeds
 # the 8 algorithmic bytes per cell by the band hand-off records.
