@@ -93,14 +93,16 @@ __host__ __device__ inline int median_ring(int W) {
     return r;
 }
 
-__device__ __forceinline__ uint32_t med3(uint32_t a, uint32_t b, uint32_t c) { return max(min(a, b), min(max(a, b), c)); }
-__device__ __forceinline__ void sort3(uint32_t a, uint32_t b, uint32_t c, uint32_t &lo, uint32_t &mi, uint32_t &hi) {
-    const uint32_t l = min(a, b), h = max(a, b);
-    lo = min(l, c);
-    hi = max(h, c);
-    mi = max(l, min(h, c));
+// Packed median helpers: two u16 map values per 32-bit word. Map values are disparities <= 511, so the sum
+// of three fits a half and the median of three is a + b + c - min - max with no half carrying or borrowing;
+// the 3-input packed minimum and maximum are single DPX instructions on sm_100+.
+__device__ __forceinline__ uint32_t pmed3(uint32_t a, uint32_t b, uint32_t c) {
+    return a + b + c - __vimin3_u16x2(a, b, c) - __vimax3_u16x2(a, b, c);
 }
-constexpr int kMedRun = 4; // consecutive median positions per thread
+// (high half of a, low half of b): the column pair shifted by one position
+__device__ __forceinline__ uint32_t shift1(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
+__device__ __forceinline__ uint32_t med3s(uint32_t a, uint32_t b, uint32_t c) { return max(min(a, b), min(max(a, b), c)); }
+constexpr int kMedPairs = 2; // packed position pairs per thread
 
 // median3x3_SSE(a, a, W, H) in place (postprocess.cpp:15-71 as called at SisterMultiviewDisparities.hpp:198
 // and siblings). Over the flattened array of N = W*H: out[x] = in[x] for x < W and x >= N-W-4;
@@ -110,6 +112,13 @@ constexpr int kMedRun = 4; // consecutive median positions per thread
 // one CTA per map sweeps the chunks in order, keeping the last 2W outputs in a shared ring. The inputs
 // a chunk reads (positions s-1 .. e+W) are staged in shared memory by cp.async kMedPF chunks ahead into
 // kMedPF+1 buffers, so the sweep never waits on global memory and needs one CTA barrier per chunk.
+// Inside a chunk the positions are taken in even-aligned pairs, two per 32-bit word: window column c of
+// position x is (out[c-W], in[c], in[c+W]); each packed column word is sorted once (packed min, median, max)
+// and the median of nine is med3(max of the column minima, med3 of the column medians, min of the column
+// maxima), the shifted columns coming from byte permutes of neighbouring words. A pair never straddles the
+// chunk end (position e depends on the chunk's first position), so an odd first position and an odd last one
+// are done one at a time. Halves of loaded words outside the chunk's columns only feed positions that are not
+// computed; they hold map values too (shared memory is zeroed first), so they cannot carry into a used half.
 constexpr int kMedPF = 3;
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
                                                       uint16_t *__restrict__ med, int k0) {
@@ -123,6 +132,10 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
     const int blen = 2 * W + 32; // staged input span of one chunk, rounded out to 16-byte boundaries
     uint16_t *ring = msm;        // ring[x & mask] = out[x] for the last 2W positions
     uint16_t *bufs = msm + rlen; // kMedPF + 1 staging buffers of blen
+    // every shared entry starts at 0, so that the halves of packed words which hold no position of the chunk
+    // (never-written entries included) are map values <= 511 like all others and no packed sum carries
+    for (int o = threadIdx.x; o < (rlen + (kMedPF + 1) * blen) / 2; o += blockDim.x) reinterpret_cast<uint32_t *>(msm)[o] = 0u;
+    __syncthreads();
     // head: x < W unchanged, x == W -> 0
     for (int x = threadIdx.x; x <= W; x += blockDim.x) {
         const uint16_t v = (x < W) ? in[x] : (uint16_t)0;
@@ -158,25 +171,49 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
         asm volatile("cp.async.commit_group;" ::: "memory");
         const int e = min(s + per, end);
         const uint16_t *bi = bufs + (size_t)(c % (kMedPF + 1)) * blen - base(s); // bi[x] = in[x] for the span
-        // kMedRun consecutive positions per thread share their window columns: column c of position x's
-        // window is (out[c-W], in[c], in[c+W]) for c = x-1..x+1; each column is sorted once and the median
-        // of nine is med3(max of the column minima, med3 of the column medians, min of the column maxima).
-        // Columns past e are not needed (clamped to e: out[e-W] belongs to an earlier chunk).
-        for (int x0 = s + threadIdx.x * kMedRun; x0 < e; x0 += blockDim.x * kMedRun) {
-            uint32_t lo[kMedRun + 2], mi[kMedRun + 2], hi[kMedRun + 2];
+        const int sp = s + (s & 1);      // first even position
+        const int np = (e - sp) >> 1;    // whole pairs in [sp, e)
+        for (int t = threadIdx.x; t * kMedPairs < np; t += blockDim.x) {
+            const int x0 = sp + 2 * kMedPairs * t;
+            // packed column words j = 0 .. kMedPairs+1 hold columns (x0 + 2j - 2, x0 + 2j - 1)
+            uint32_t lo[kMedPairs + 2], mi[kMedPairs + 2], hi[kMedPairs + 2];
 #pragma unroll
-            for (int k = 0; k < kMedRun + 2; k++) {
-                const int cx = min(x0 - 1 + k, e);
-                sort3(ring[(cx - W) & mask], bi[cx], bi[cx + W], lo[k], mi[k], hi[k]);
+            for (int j = 0; j < kMedPairs + 2; j++) {
+                const int cx = x0 + 2 * j - 2;
+                const uint32_t top = *reinterpret_cast<const uint32_t *>(ring + ((cx - W) & mask));
+                const uint32_t mid = *reinterpret_cast<const uint32_t *>(bi + cx);
+                const uint32_t bot = *reinterpret_cast<const uint32_t *>(bi + cx + W);
+                lo[j] = __vimin3_u16x2(top, mid, bot);
+                hi[j] = __vimax3_u16x2(top, mid, bot);
+                mi[j] = top + mid + bot - lo[j] - hi[j];
             }
 #pragma unroll
-            for (int j = 0; j < kMedRun; j++) {
-                const int x = x0 + j;
-                if (x >= e) break;
-                const uint32_t l3 = max(lo[j], max(lo[j + 1], lo[j + 2]));
-                const uint32_t m3 = med3(mi[j], mi[j + 1], mi[j + 2]);
-                const uint32_t h3 = min(hi[j], min(hi[j + 1], hi[j + 2]));
-                const uint32_t v = med3(l3, m3, h3);
+            for (int j = 0; j < kMedPairs; j++) {
+                const int x = x0 + 2 * j;
+                if (x >= sp + 2 * np) break;
+                const uint32_t l3 = __vimax3_u16x2(shift1(lo[j], lo[j + 1]), lo[j + 1], shift1(lo[j + 1], lo[j + 2]));
+                const uint32_t m3 = pmed3(shift1(mi[j], mi[j + 1]), mi[j + 1], shift1(mi[j + 1], mi[j + 2]));
+                const uint32_t h3 = __vimin3_u16x2(shift1(hi[j], hi[j + 1]), hi[j + 1], shift1(hi[j + 1], hi[j + 2]));
+                const uint32_t v = pmed3(l3, m3, h3);
+                *reinterpret_cast<uint32_t *>(ring + (x & mask)) = v;
+                *reinterpret_cast<uint32_t *>(out + x) = v;
+            }
+        }
+        // an odd first position and an odd last one, one at a time (columns x-1 .. x+1, none past e)
+        if (threadIdx.x == blockDim.x - 1) {
+            for (int q = 0; q < 2; q++) {
+                const int x = q == 0 ? ((s & 1) ? s : -1) : (((e - sp) & 1) ? e - 1 : -1);
+                if (x < 0) continue;
+                uint32_t l[3], m[3], h[3];
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const int cx = min(x - 1 + j, e);
+                    const uint32_t a0 = ring[(cx - W) & mask], a1 = bi[cx], a2 = bi[cx + W];
+                    l[j] = min(min(a0, a1), a2);
+                    h[j] = max(max(a0, a1), a2);
+                    m[j] = med3s(a0, a1, a2);
+                }
+                const uint32_t v = med3s(max(l[0], max(l[1], l[2])), med3s(m[0], m[1], m[2]), min(h[0], min(h[1], h[2])));
                 ring[x & mask] = (uint16_t)v;
                 out[x] = (uint16_t)v;
             }
@@ -234,7 +271,10 @@ void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaS
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
-    median_kernel<<<2 * nf, 1024, smem, st>>>(wta, g, med, 2 * f0);
+    // one thread per kMedPairs position pairs of a chunk (W-1 positions), plus one for the odd ends
+    int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
+    threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
+    median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0);
 }
 
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {
