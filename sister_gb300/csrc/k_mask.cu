@@ -11,36 +11,42 @@ namespace {
 //   L(a) = min over b of key(a, b)   (d = a - b <= min(a, D-1))
 //   R(b) = min over a of key(a, b)   (k = a - b <= min(D-1, W-1-b))
 // so every cell is counted once. A warp owns 32 consecutive columns b (one per lane) and walks the
-// diagonals d = 0..D-1, two per step: lane l keeps R of its column in a register and carries the partial L
+// diagonals d = 0..D-1, four per step: lane l keeps R of its column in a register and carries the partial L
 // of row a = b0+l+d, which moves down the lanes as d grows; rows whose cells in this block are all seen are
 // merged into a shared array with atomicMin.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
 // One CTA per frame row; both census rows staged in shared memory.
-// Two diagonals per step: lane l meets cells (b0+l+d, b0+l) and (b0+l+d+1, b0+l). Before the step lane l
-// carries the partial L of row a = b0+l+d; that row gets the first cell of lane l and the second cell of
-// lane l-1. After the step the rows of lanes 0 and 1 have no later cell in this block: they are merged and
-// the partials move two lanes down (lane 31's second cell starts the row that enters at lane 30). dmax is
-// even (D is a multiple of 8, W - b0 a multiple of 4).
+// Four diagonals per step: lane l meets cells (b0+l+d+i, b0+l) for i = 0..3. Before the step lane l carries
+// the partial L of row a = b0+l+d; that row gets cell i of lane l-i (i <= l). A shuffle of cell i from lane
+// (l-i) mod 32 hands lane l either a cell of its own row (i <= l) or, wrapping around, a cell of the row that
+// enters the warp at lane 28+l after the step (i > l: cells of lanes 29..31). After the step the rows of lanes
+// 0..3 have no later cell in this block: they are merged into shared memory and the partials move four lanes
+// down, lanes 28..31 taking the entering rows. dmax is a multiple of 4 (D is a multiple of 8, W - b0 of 4).
 template <bool EDGE>
 __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b0, int lane, int W, int dmax,
                                           uint32_t *lk, uint32_t &racc) {
     uint32_t lacc = 0xFFFFFFFFu;
     const int b = b0 + lane;
+    // OR masks: a shuffled cell i counts for this lane's row when i <= lane, else for the entering row
+    const uint32_t m1 = lane >= 1 ? 0u : ~0u, m2 = lane >= 2 ? 0u : ~0u, m3 = lane >= 3 ? 0u : ~0u;
 #pragma unroll 2
-    for (int d = 0; d < dmax; d += 2) {
+    for (int d = 0; d < dmax; d += 4) {
         const int a = b + d;
-        uint32_t k0 = 0xFFFFFFFFu, k1 = 0xFFFFFFFFu;
-        if (!EDGE || a < W) k0 = ((uint32_t)__popcll(cc[EDGE ? min(a, W - 1) : a] ^ cb) << 16) | (uint32_t)d;
-        if (!EDGE || a + 1 < W)
-            k1 = ((uint32_t)__popcll(cc[EDGE ? min(a + 1, W - 1) : a + 1] ^ cb) << 16) | (uint32_t)(d + 1);
-        racc = min(racc, min(k0, k1));
-        // second cell of lane l-1 (lane 0 receives lane 31's, whose row enters the warp at lane 30 below)
-        const uint32_t k1rot = __shfl_sync(0xFFFFFFFFu, k1, (lane + 31) & 31);
-        lacc = min(lacc, min(k0, lane == 0 ? 0xFFFFFFFFu : k1rot));
-        if (lane < 2) atomicMin(&lk[b0 + d + lane], lacc); // rows b0+d, b0+d+1: complete for this block
-        // move the partials two lanes down; lanes 30, 31 take lane 31's second cell and a fresh row
-        const uint32_t y = lane == 0 ? k1rot : (lane == 1 ? 0xFFFFFFFFu : lacc);
-        lacc = __shfl_sync(0xFFFFFFFFu, y, (lane + 2) & 31);
+        uint32_t k[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint64_t x = cc[EDGE ? min(a + i, W - 1) : a + i] ^ cb;
+            k[i] = ((uint32_t)__popcll(x) << 16) | (uint32_t)(d + i);
+            if (EDGE && a + i >= W) k[i] = 0xFFFFFFFFu;
+        }
+        racc = __vimin3_u32(racc, __vimin3_u32(k[0], k[1], k[2]), k[3]);
+        const uint32_t s1 = __shfl_sync(0xFFFFFFFFu, k[1], (lane + 31) & 31);
+        const uint32_t s2 = __shfl_sync(0xFFFFFFFFu, k[2], (lane + 30) & 31);
+        const uint32_t s3 = __shfl_sync(0xFFFFFFFFu, k[3], (lane + 29) & 31);
+        lacc = __vimin3_u32(__vimin3_u32(lacc, k[0], s1 | m1), s2 | m2, s3 | m3);
+        const uint32_t ent = __vimin3_u32(s1 | ~m1, s2 | ~m2, s3 | ~m3);
+        if (lane < 4) atomicMin(&lk[b0 + d + lane], lacc); // rows b0+d .. b0+d+3: complete for this block
+        lacc = __shfl_sync(0xFFFFFFFFu, lane < 4 ? ent : lacc, (lane + 4) & 31);
     }
     // lane l now carries row a = b0 + l + dmax, which may still have cells in later diagonals of other blocks
     if (b + dmax < W && lacc != 0xFFFFFFFFu) atomicMin(&lk[b + dmax], lacc);
