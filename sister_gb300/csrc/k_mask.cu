@@ -5,6 +5,20 @@
 namespace sister {
 namespace {
 
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // WTALeft_SSE / WTARight_SSE with uniqueness 1 (postprocess.cpp:74-315) on a pair's Hamming volume
 // (census.cpp:54-146), without materialising the volume. Both reduce to the lowest-index argmin of the
 // same keys key(a, b) = popc(Cc[a] ^ Cn[b]) << 16 | (a - b) over the band 0 <= a - b < D:
@@ -52,8 +66,11 @@ __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b
     if (b + dmax < W && lacc != 0xFFFFFFFFu) atomicMin(&lk[b + dmax], lacc);
 }
 
+// With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
+// i] = epoch (release), so that the frame's median can start on the first rows while later rows are computed.
 __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
-                                                       uint16_t *__restrict__ wta, int f0) {
+                                                       uint16_t *__restrict__ wta, int f0, unsigned *rowflags,
+                                                       unsigned epoch) {
     extern __shared__ uint64_t srow[];
     const int f = f0 + blockIdx.y;
     const int H = g.frows(f), W = g.fcols(f), D = g.dc;
@@ -66,30 +83,37 @@ __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restric
             L[j] = 0;
             R[j] = 0;
         }
-        return;
+    } else {
+        uint64_t *cc = srow, *cn = srow + W;
+        uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W);
+        const uint64_t *gc = census + (size_t)(2 * f) * g.plane + (size_t)i * W;
+        const uint64_t *gn = census + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
+        for (int j = threadIdx.x; j < W; j += blockDim.x) {
+            cc[j] = gc[j];
+            cn[j] = gn[j];
+            lk[j] = 0xFFFFFFFFu;
+        }
+        __syncthreads();
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int blk = warp; blk * 32 < W; blk += nw) {
+            const int b0 = 32 * blk, b = b0 + lane;
+            const uint64_t cb = cn[min(b, W - 1)];
+            const int dmax = min(D, W - b0);
+            uint32_t racc = 0xFFFFFFFFu;
+            if (b0 + 31 + dmax - 1 < W) wta_block<false>(cc, cb, b0, lane, W, dmax, lk, racc);
+            else wta_block<true>(cc, cb, b0, lane, W, dmax, lk, racc);
+            if (b < W) R[b] = (uint16_t)(racc & 0xFFFFu);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < W; j += blockDim.x) L[j] = (uint16_t)(lk[j] & 0xFFFFu);
     }
-    uint64_t *cc = srow, *cn = srow + W;
-    uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W);
-    const uint64_t *gc = census + (size_t)(2 * f) * g.plane + (size_t)i * W;
-    const uint64_t *gn = census + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
-    for (int j = threadIdx.x; j < W; j += blockDim.x) {
-        cc[j] = gc[j];
-        cn[j] = gn[j];
-        lk[j] = 0xFFFFFFFFu;
+    if (rowflags) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_u32(rowflags + (size_t)f * max(g.Wp, g.Hp) + i, epoch);
+        }
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int blk = warp; blk * 32 < W; blk += nw) {
-        const int b0 = 32 * blk, b = b0 + lane;
-        const uint64_t cb = cn[min(b, W - 1)];
-        const int dmax = min(D, W - b0);
-        uint32_t racc = 0xFFFFFFFFu;
-        if (b0 + 31 + dmax - 1 < W) wta_block<false>(cc, cb, b0, lane, W, dmax, lk, racc);
-        else wta_block<true>(cc, cb, b0, lane, W, dmax, lk, racc);
-        if (b < W) R[b] = (uint16_t)(racc & 0xFFFFu);
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < W; j += blockDim.x) L[j] = (uint16_t)(lk[j] & 0xFFFFu);
 }
 
 // shared ring length for the median sweep: a power of two >= 2W
@@ -125,9 +149,13 @@ constexpr int kMedPairs = 2; // packed position pairs per thread
 // chunk end (position e depends on the chunk's first position), so an odd first position and an odd last one
 // are done one at a time. Halves of loaded words outside the chunk's columns only feed positions that are not
 // computed; they hold map values too (shared memory is zeroed first), so they cannot carry into a used half.
+// With rowflags the kernel may run while the frame's pair WTA is still writing the map: before input rows are
+// read (the head, each chunk's staging, the tail) warp 0 waits until they are published with this epoch,
+// and a CTA barrier passes that on. The wait is bounded: on expiry the error flag is raised and the sweep goes on.
 constexpr int kMedPF = 3;
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
-                                                      uint16_t *__restrict__ med, int k0) {
+                                                      uint16_t *__restrict__ med, int k0, const unsigned *rowflags,
+                                                      unsigned epoch, unsigned *err) {
     extern __shared__ __align__(16) uint16_t msm[];
     const int k = k0 + blockIdx.x, f = k >> 1;
     const int H = g.frows(f), W = g.fcols(f);
@@ -141,6 +169,32 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
     // every shared entry starts at 0, so that the halves of packed words which hold no position of the chunk
     // (never-written entries included) are map values <= 511 like all others and no packed sum carries
     for (int o = threadIdx.x; o < (rlen + (kMedPF + 1) * blen) / 2; o += blockDim.x) reinterpret_cast<uint32_t *>(msm)[o] = 0u;
+    const unsigned *flags = rowflags ? rowflags + (size_t)f * max(g.Wp, g.Hp) : nullptr;
+    int ready = 0; // (warp 0) input rows known to be published
+    // warp 0 reads 32 consecutive row flags per poll and advances past the leading published ones
+    auto wait_rows = [&](int last) {
+        if (!flags || threadIdx.x >= 32) return;
+        const int lane = threadIdx.x;
+        last = min(last, H - 1);
+        const unsigned long long t0 = global_ns();
+        for (unsigned n = 1; ready <= last; n++) {
+            const int r = ready + lane;
+            const unsigned ok = __ballot_sync(0xFFFFFFFFu, r >= H || ld_acquire_u32(flags + r) == epoch);
+            ready += (ok == 0xFFFFFFFFu) ? 32 : __ffs(~ok) - 1;
+            if (ready > last) break;
+            __nanosleep(100);
+            if (n % 64 == 0) {
+                // one lane decides, so that `ready` stays the same in every lane
+                const bool expired =
+                    lane == 0 && (*(volatile unsigned *)err != kErrNone || global_ns() - t0 > 2000000000ull);
+                if (__any_sync(0xFFFFFFFFu, expired)) {
+                    if (lane == 0) atomicCAS(err, kErrNone, kErrTimeout);
+                    ready = H;
+                }
+            }
+        }
+    };
+    wait_rows(0);
     __syncthreads();
     // head: x < W unchanged, x == W -> 0
     for (int x = threadIdx.x; x <= W; x += blockDim.x) {
@@ -148,10 +202,10 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
         out[x] = v;
         ring[x & mask] = v;
     }
-    // tail: x >= N-W-4 unchanged
-    for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
     const int end = N - W - 4;
     const int per = W - 1;
+    // last input row a chunk starting at sc reads (its staged span ends below b1)
+    auto span_row = [&](int sc) { return (min(N, (min(sc + per, end) + W + 1 + 7) & ~7) - 1) / W; };
     // chunk c covers [W+1 + c*per, min(+per, end)); its inputs span [s-1, e+W+1), staged from base(c)
     auto base = [&](int sc) { return (sc - 1) & ~7; };
     auto stage = [&](int sc, uint16_t *dst) {
@@ -163,6 +217,8 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
                          "l"(in + b0 + o)
                          : "memory");
     };
+    wait_rows(span_row(W + 1 + (kMedPF - 1) * per));
+    __syncthreads();
     for (int c = 0; c < kMedPF; c++) {
         stage(W + 1 + c * per, bufs + (size_t)c * blen);
         asm volatile("cp.async.commit_group;" ::: "memory");
@@ -170,8 +226,9 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
     int c = 0;
     for (int s = W + 1; s < end; s += per, c++) {
         asm volatile("cp.async.wait_group %0;" ::"n"(kMedPF - 1) : "memory");
+        if (s + kMedPF * per < end) wait_rows(span_row(s + kMedPF * per));
         // this chunk's inputs (every thread's copies) are in, the previous chunk's outputs are in the ring,
-        // and the buffer of chunk c-1 is free for chunk c+kMedPF
+        // the buffer of chunk c-1 is free for chunk c+kMedPF and that chunk's input rows are published
         __syncthreads();
         stage(s + kMedPF * per, bufs + (size_t)((c + kMedPF) % (kMedPF + 1)) * blen);
         asm volatile("cp.async.commit_group;" ::: "memory");
@@ -226,6 +283,10 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // tail: x >= N-W-4 unchanged
+    wait_rows(H - 1);
+    __syncthreads();
+    for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
 }
 
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) and the mask loops of SisterMultiviewDisparities.hpp:201-251:
@@ -268,19 +329,21 @@ void init_mask_kernels() {
     cudaGetLastError();
 }
 
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0, int nf) {
+void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0, int nf,
+                     unsigned *rowflags, unsigned epoch) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
-    pair_wta_kernel<<<dim3(mx, nf), 256, smem, st>>>(census, g, wta, f0);
+    pair_wta_kernel<<<dim3(mx, nf), 256, smem, st>>>(census, g, wta, f0, rowflags, epoch);
 }
 
-void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf) {
+void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf,
+                   const unsigned *rowflags, unsigned epoch, unsigned *err) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     // one thread per kMedPairs position pairs of a chunk (W-1 positions), plus one for the odd ends
     int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
     threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
-    median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0);
+    median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err);
 }
 
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {

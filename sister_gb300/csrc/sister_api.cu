@@ -66,6 +66,9 @@ struct sister_ctx {
     bool loaded = false;
     int w = 0, h = 0, dc = 0;
     DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, sum1, bnd, progress, errflag, disp, outs;
+    // pair WTA row flags: [4][max(Wp, Hp)] u32 holding the epoch (compute count) in which the row was written
+    DevBuf rowflags;
+    unsigned epoch = 0;
     SgmPlan plan{};
     int plan_w = 0, plan_h = 0, plan_dc = 0;
     int tune_rows = 0, tune_cs = 0;
@@ -197,6 +200,11 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         cudaError_t e = r.b->ensure(r.bytes);
         if (e != cudaSuccess) return c->cuda_fail(e, r.what);
     }
+    // a new flag array starts at 0, which no epoch takes
+    void *old = c->rowflags.p;
+    cudaError_t e = c->rowflags.ensure(4 * (size_t)std::max(g.Wp, g.Hp) * sizeof(unsigned));
+    if (e == cudaSuccess && c->rowflags.p != old) e = cudaMemsetAsync(c->rowflags.p, 0, c->rowflags.cap, c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "row flags");
     return SISTER_OK;
 }
 
@@ -220,15 +228,22 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     c->mark(SISTER_STAGE_FRAMES);
     launch_census(c->frames.as<uint8_t>(), g, c->census.as<uint64_t>(), st);
     c->mark(SISTER_STAGE_CENSUS);
-    // frames 90/270 first: their medians sweep the most chunks (rows of Wp); each frame's median and mask
-    // overlap the remaining frames' pair WTA. With profiling on, the median stage reports the time the
-    // medians and masks extend past the last pair WTA.
+    // frames 90/270 first: their medians sweep the most chunks (rows of Wp). Each frame's median starts with
+    // the frame's pair WTA on a side stream and follows it row by row (the pair WTA publishes every finished
+    // row with this compute's epoch), so it overlaps its own frame's WTA and the later frames'; the masks
+    // follow the median on the same stream. With profiling on, the median stage reports the time the medians
+    // and masks extend past the last pair WTA.
+    // A waiting kernel is always submitted after the kernel it waits for: streams may share a hardware queue, in
+    // which work runs in submission order, so a median submitted before its pair WTA could hold that WTA back.
+    if (++c->epoch == 0) c->epoch = 1;
     static const int order[4] = {1, 3, 0, 2};
     for (int f : order) {
-        launch_pair_wta(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), st, f, 1);
         cudaEventRecord(c->ev_wta[f], st);
+        launch_pair_wta(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), st, f, 1, c->rowflags.as<unsigned>(),
+                        c->epoch);
         cudaStreamWaitEvent(c->side[f], c->ev_wta[f], 0);
-        launch_median(c->wta.as<uint16_t>(), g, c->med.as<uint16_t>(), c->side[f], f, 1);
+        launch_median(c->wta.as<uint16_t>(), g, c->med.as<uint16_t>(), c->side[f], f, 1, c->rowflags.as<unsigned>(),
+                      c->epoch, c->errflag.as<unsigned>());
         launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), c->side[f], f, 1);
         cudaEventRecord(c->ev_mask[f], c->side[f]);
     }
@@ -266,7 +281,8 @@ int read_device_error(sister_ctx *c) {
     cudaError_t e = cudaMemcpy(&flag, c->errflag.p, sizeof flag, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return c->cuda_fail(e, "reading device error flag");
     if (flag == kErrTimeout)
-        return c->fail(SISTER_ETIMEOUT, "aggregation band hand-off wait expired (device reported timeout)");
+        return c->fail(SISTER_ETIMEOUT, "a bounded device wait expired (aggregation band hand-off or median row "
+                                        "flags; device reported timeout)");
     return SISTER_OK;
 }
 

@@ -75,8 +75,12 @@ void launch_to_gray(const uint8_t *const src[5], int stride, int channels, int w
 void launch_frames(const uint8_t *views_dev, const Geom &g, uint8_t *frames, cudaStream_t st);
 void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st);
 // the mask stages run on frames [f0, f0 + nf) (all four by default)
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4);
-void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4);
+// rowflags (4 x max(Wp, Hp) u32, or null): pair WTA publishes each frame row with `epoch`; a median given the
+// same flags waits for the rows it reads, so it may be launched before the frame's pair WTA has finished.
+void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4,
+                     unsigned *rowflags = nullptr, unsigned epoch = 0);
+void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4,
+                   const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr);
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
