@@ -68,14 +68,10 @@ __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b
 
 // With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
 // i] = epoch (release), so that the frame's median can start on the first rows while later rows are computed.
-__global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
-                                                       uint16_t *__restrict__ wta, int f0, unsigned *rowflags,
-                                                       unsigned epoch) {
-    extern __shared__ uint64_t srow[];
-    const int f = f0 + blockIdx.y;
+__device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census, const Geom &g,
+                                             uint16_t *__restrict__ wta, int f, int i, unsigned *rowflags,
+                                             unsigned epoch, uint64_t *srow) {
     const int H = g.frows(f), W = g.fcols(f), D = g.dc;
-    const int i = blockIdx.x;
-    if (i >= H) return;
     uint16_t *L = wta + (size_t)(2 * f) * g.plane + (size_t)i * W;
     uint16_t *R = wta + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
     if (i < 3 || i >= H - 2) {
@@ -116,6 +112,15 @@ __global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restric
     }
 }
 
+__global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
+                                                       uint16_t *__restrict__ wta, int f0, unsigned *rowflags,
+                                                       unsigned epoch) {
+    extern __shared__ uint64_t srow[];
+    const int f = f0 + blockIdx.y;
+    if ((int)blockIdx.x >= g.frows(f)) return;
+    pair_wta_row(census, g, wta, f, blockIdx.x, rowflags, epoch, srow);
+}
+
 // shared ring length for the median sweep: a power of two >= 2W
 __host__ __device__ inline int median_ring(int W) {
     int r = 1;
@@ -153,11 +158,10 @@ constexpr int kMedPairs = 2; // packed position pairs per thread
 // read (the head, each chunk's staging, the tail) warp 0 waits until they are published with this epoch,
 // and a CTA barrier passes that on. The wait is bounded: on expiry the error flag is raised and the sweep goes on.
 constexpr int kMedPF = 3;
-__global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
-                                                      uint16_t *__restrict__ med, int k0, const unsigned *rowflags,
-                                                      unsigned epoch, unsigned *err) {
-    extern __shared__ __align__(16) uint16_t msm[];
-    const int k = k0 + blockIdx.x, f = k >> 1;
+__device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, const Geom &g, uint16_t *__restrict__ med,
+                                           int k, const unsigned *rowflags, unsigned epoch, unsigned *err,
+                                           uint16_t *msm) {
+    const int f = k >> 1;
     const int H = g.frows(f), W = g.fcols(f);
     const int N = W * H; // a multiple of 16 (W and H are multiples of 4)
     const uint16_t *in = wta + (size_t)k * g.plane;
@@ -289,6 +293,42 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
     for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
 }
 
+__global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
+                                                      uint16_t *__restrict__ med, int k0, const unsigned *rowflags,
+                                                      unsigned epoch, unsigned *err) {
+    extern __shared__ __align__(16) uint16_t msm[];
+    median_map(wta, g, med, k0 + blockIdx.x, rowflags, epoch, err, msm);
+}
+
+// Both WTAs of every frame row and the eight medians in one launch: blocks 0..7 sweep the medians of maps
+// 0..7 and follow the rows as the other blocks publish them (row flags). The rows of the four frames are
+// interleaved in proportion to their counts (frames 1 and 3 have Wp rows, frames 0 and 2 have Hp), so every
+// median receives its rows at a steady rate and all eight finish close to the last row. Blocks are dispatched
+// in index order in practice, so the medians start with the first rows; nothing waits on a median, so any
+// dispatch order completes.
+__global__ void __launch_bounds__(1024) wta_median_kernel(const uint64_t *__restrict__ census, Geom g,
+                                                          uint16_t *__restrict__ wta, uint16_t *__restrict__ med,
+                                                          unsigned *rowflags, unsigned epoch, unsigned *err) {
+    extern __shared__ __align__(16) uint64_t fsm[];
+    if (blockIdx.x < 8) {
+        median_map(wta, g, med, blockIdx.x, rowflags, epoch, err, reinterpret_cast<uint16_t *>(fsm));
+        return;
+    }
+    // row t of the merged sequence: A = rows of frames 1 and 3 (2 Wp), B = rows of frames 0 and 2 (2 Hp)
+    const long long t = blockIdx.x - 8, na = 2LL * g.Wp, tot = na + 2LL * g.Hp;
+    const long long a0 = t * na / tot, a1 = (t + 1) * na / tot; // A items before t, and up to t
+    int f, i;
+    if (a1 > a0) {
+        f = (a0 & 1) ? 3 : 1;
+        i = (int)(a0 >> 1);
+    } else {
+        const long long b = t - a0;
+        f = (b & 1) ? 2 : 0;
+        i = (int)(b >> 1);
+    }
+    pair_wta_row(census, g, wta, f, i, rowflags, epoch, fsm);
+}
+
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) and the mask loops of SisterMultiviewDisparities.hpp:201-251:
 // keep = L <= j && |L - R[j-L]| <= 5; mask = keep && L > 0 && j >= dc; written in padded original
 // coordinates (frame 2: (i, Wp-1-j); frame 1: transpose + flip(-1); frame 3: transpose + flip(1)).
@@ -326,6 +366,8 @@ void init_mask_kernels() {
     cudaFuncAttributes fa{};
     cudaFuncGetAttributes(&fa, median_kernel); // its mbarriers are static shared memory
     cudaFuncSetAttribute(median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    cudaFuncGetAttributes(&fa, wta_median_kernel);
+    cudaFuncSetAttribute(wta_median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
     cudaGetLastError();
 }
 
@@ -344,6 +386,18 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
     int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
     threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
     median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err);
+}
+
+void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
+                       unsigned epoch, unsigned *err, cudaStream_t st) {
+    const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
+    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
+    const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
+    int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
+    threads = threads < 256 ? 256 : threads > 1024 ? 1024 : threads;
+    const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
+    wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
+                                                                                       epoch, err);
 }
 
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {

@@ -58,10 +58,6 @@ struct sister_ctx {
     int num_sms = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    // per-frame side streams: a frame's median and masks run as soon as its pair WTA is done, while the
-    // pair WTA of the other frames proceeds on the main stream
-    cudaStream_t side[4] = {};
-    cudaEvent_t ev_wta[4] = {}, ev_mask[4] = {};
     std::string err;
     bool loaded = false;
     int w = 0, h = 0, dc = 0;
@@ -228,28 +224,15 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     c->mark(SISTER_STAGE_FRAMES);
     launch_census(c->frames.as<uint8_t>(), g, c->census.as<uint64_t>(), st);
     c->mark(SISTER_STAGE_CENSUS);
-    // frames 90/270 first: their medians sweep the most chunks (rows of Wp). Each frame's median starts with
-    // the frame's pair WTA on a side stream and follows it row by row (the pair WTA publishes every finished
-    // row with this compute's epoch), so it overlaps its own frame's WTA and the later frames'; the masks
-    // follow the median on the same stream. With profiling on, the median stage reports the time the medians
-    // and masks extend past the last pair WTA.
-    // A waiting kernel is always submitted after the kernel it waits for: streams may share a hardware queue, in
-    // which work runs in submission order, so a median submitted before its pair WTA could hold that WTA back.
+    // Pair WTA of the four frames and the eight medians in one launch: the median blocks come first and follow
+    // the WTA rows as they are published (each row with this compute's epoch); the masks follow. With
+    // profiling on, the pair WTA stage covers that launch and the median stage is empty.
     if (++c->epoch == 0) c->epoch = 1;
-    static const int order[4] = {1, 3, 0, 2};
-    for (int f : order) {
-        cudaEventRecord(c->ev_wta[f], st);
-        launch_pair_wta(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), st, f, 1, c->rowflags.as<unsigned>(),
-                        c->epoch);
-        cudaStreamWaitEvent(c->side[f], c->ev_wta[f], 0);
-        launch_median(c->wta.as<uint16_t>(), g, c->med.as<uint16_t>(), c->side[f], f, 1, c->rowflags.as<unsigned>(),
-                      c->epoch, c->errflag.as<unsigned>());
-        launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), c->side[f], f, 1);
-        cudaEventRecord(c->ev_mask[f], c->side[f]);
-    }
+    launch_wta_median(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), c->med.as<uint16_t>(),
+                      c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st);
     c->mark(SISTER_STAGE_PAIR_WTA);
-    for (int f = 0; f < 4; f++) cudaStreamWaitEvent(st, c->ev_mask[f], 0);
     c->mark(SISTER_STAGE_MEDIAN);
+    launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
     c->mark(SISTER_STAGE_MASKS);
     e = cudaGetLastError();
     if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
@@ -311,15 +294,6 @@ int sister_ctx_create(sister_ctx **out, int device) {
         return SISTER_EDEVICE;
     }
     c->stream = c->own_stream;
-    for (int f = 0; f < 4; f++) {
-        if (cudaStreamCreateWithFlags(&c->side[f], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->ev_wta[f], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->ev_mask[f], cudaEventDisableTiming) != cudaSuccess) {
-            cudaGetLastError();
-            sister_ctx_destroy(c);
-            return SISTER_EDEVICE;
-        }
-    }
     init_device_kernels(device);
     if (c->errflag.ensure(sizeof(unsigned)) != cudaSuccess) {
         delete c;
@@ -333,14 +307,6 @@ void sister_ctx_destroy(sister_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
-    for (int f = 0; f < 4; f++) {
-        if (c->side[f]) {
-            cudaStreamSynchronize(c->side[f]);
-            cudaStreamDestroy(c->side[f]);
-        }
-        if (c->ev_wta[f]) cudaEventDestroy(c->ev_wta[f]);
-        if (c->ev_mask[f]) cudaEventDestroy(c->ev_mask[f]);
-    }
     if (c->own_stream) {
         cudaStreamSynchronize(c->own_stream);
         cudaStreamDestroy(c->own_stream);

@@ -81,6 +81,9 @@ void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaS
                      unsigned *rowflags = nullptr, unsigned epoch = 0);
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4,
                    const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr);
+// pair WTA of every frame and the eight medians in one launch (medians follow the rows through rowflags)
+void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
+                       unsigned epoch, unsigned *err, cudaStream_t st);
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
