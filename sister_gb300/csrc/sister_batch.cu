@@ -40,7 +40,8 @@ RigBytes rig_bytes(int w, int h, int dc, int channels, int R) {
     RigBytes b;
     const size_t plane = g.plane;
     b.prep = al(channels == 3 ? 5 * (size_t)w * h * 3 : 0) + al(5 * (size_t)w * h) + al(8 * plane) +
-             al(8 * plane * 8) + 2 * al(8 * plane * 2) + al(4 * plane);
+             al(8 * plane * 8) + 2 * al(8 * plane * 2) + al(4 * plane) +
+             al(4 * (size_t)std::max(g.Wp, g.Hp) * sizeof(unsigned)); // pair WTA row flags
     const size_t nbands = (size_t)(g.Hp + R - 1) / R;
     const size_t vol = plane * g.dp * 2;
     b.per_mode = 3 * al(vol) + al(2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2) + al(progress_bytes(2 * nbands)) +
@@ -113,7 +114,9 @@ int validate(sister_batch *b, const sister_rig &r, int k) {
 int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
     b->top = 0;
     unsigned *errflag = b->take<unsigned>(sizeof(unsigned));
+    // the rigs' streams read and raise this flag: clear it before any of them starts
     cudaError_t e = cudaMemsetAsync(errflag, 0, sizeof(unsigned), b->main);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->main);
     if (e != cudaSuccess) return b->cuda_fail(e, "reset error flag");
     std::vector<Job> jobs;
     for (int k = first; k < last; k++) {
@@ -147,10 +150,14 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
         uint16_t *wta = b->take<uint16_t>(8 * plane * 2);
         uint16_t *med = b->take<uint16_t>(8 * plane * 2);
         uint8_t *masks = b->take<uint8_t>(4 * plane);
+        // row flags of the pair WTA / median launch: a fresh array starts at 0 and epoch 1 marks a written row
+        const size_t flag_bytes = 4 * (size_t)std::max(g.Wp, g.Hp) * sizeof(unsigned);
+        unsigned *rowflags = b->take<unsigned>(flag_bytes);
+        e = cudaMemsetAsync(rowflags, 0, flag_bytes, st);
+        if (e != cudaSuccess) return b->cuda_fail(e, "reset row flags");
         launch_frames(views, g, frames, st);
         launch_census(frames, g, census, st);
-        launch_pair_wta(census, g, wta, st);
-        launch_median(wta, g, med, st);
+        launch_wta_median(census, g, wta, med, rowflags, 1u, errflag, st);
         launch_lrc_mask(med, g, masks, st);
         const int R = sgm_rows_max(g.dp, b->device);
         uint16_t *outs[3] = {r.multi, r.horiz, r.vert};
