@@ -67,6 +67,16 @@ SISTER_API int sister_set_max_disparity(sister_ctx *ctx, int dc);
  * buffers. `multi` is mode 0 (all four pairs), `horiz` mode 1, `vert` mode 2; any may be NULL and the
  * corresponding aggregation is then skipped. Blocks until the results are on the host. */
 SISTER_API int sister_compute(sister_ctx *ctx, uint16_t *multi, uint16_t *horiz, uint16_t *vert);
+
+/* Two-view stereo of the reference's doStereo (SisterMultiviewDisparities.hpp:122-150; dead code there, offered
+ * here as the same pipeline for one image pair): census of both images, Hamming cost volume, the 8-path
+ * aggregation, WTA-left and WTA-right, in-place 3x3 medians of both maps and the LR check (threshold 5), on the
+ * images as given (no padding). center and other: host gray images (width x height, row stride `stride`), other
+ * being the image searched at (y, x - d) like the multiview right view. Outputs (host, width*height each): left =
+ * the checked left disparities, -10 where rejected (the reference's float map holds the same integers); right =
+ * the median-filtered right map. Same size and dc rules as sister_compute. */
+SISTER_API int sister_stereo(sister_ctx *ctx, const uint8_t *center, const uint8_t *other, int width, int height,
+                             int stride, int dc, int16_t *left, uint16_t *right);
 /* Same with device output pointers; asynchronous on the context stream (see sister_synchronize). */
 SISTER_API int sister_compute_device(sister_ctx *ctx, uint16_t *multi, uint16_t *horiz, uint16_t *vert);
 

@@ -140,6 +140,34 @@ class Port(_Lib):
         self.lib.orc_masked_cost(carr, marr, Wp, Hp, dc, int(mode), _ptr(M, _u16p))
         return M
 
+    def wta_right_vol(self, vol):
+        vol = np.ascontiguousarray(vol, np.uint16)
+        H, W, D = vol.shape
+        out = np.zeros((H, W), np.uint16)
+        self.lib.orc_wta_right_vol(_ptr(vol, _u16p), W, H, D, _ptr(out, _u16p))
+        return out
+
+    def lrcheck(self, L, R):
+        L = np.ascontiguousarray(L, np.uint16)
+        R = np.ascontiguousarray(R, np.uint16)
+        H, W = L.shape
+        out = np.zeros((H, W), np.int16)
+        self.lib.orc_lrcheck(_ptr(L, _u16p), _ptr(R, _u16p), W, H, _ptr(out, ctypes.POINTER(ctypes.c_int16)))
+        return out
+
+    def stereo(self, center, other, D):
+        """doStereo: (L with -10 where the LR check rejects, median-filtered R)."""
+        a = np.ascontiguousarray(center, np.uint8)
+        b = np.ascontiguousarray(other, np.uint8)
+        h, w = a.shape
+        L = np.zeros((h, w), np.int16)
+        R = np.zeros((h, w), np.uint16)
+        rc = self.lib.orc_stereo(_ptr(a, _u8p), _ptr(b, _u8p), w, h, D, _ptr(L, ctypes.POINTER(ctypes.c_int16)),
+                                 _ptr(R, _u16p))
+        if rc:
+            raise MemoryError("oracle stereo: out of memory")
+        return L, R
+
     def wta_left_vol(self, vol):
         vol = np.ascontiguousarray(vol, np.uint16)
         H, W, D = vol.shape
@@ -211,6 +239,14 @@ class Ref(_Lib):
         S = np.zeros_like(C)
         self.lib.ref_sgm(_ptr(C, _u16p), W, H, D, _ptr(S, _u16p))
         return S
+
+    def stereo(self, center, other, D):
+        """doStereo (hpp:122-150) from the reference's own stages: ad_census, sgm, WTALeft / WTARight, in-place
+        medians, doLRCheck. Returns (L as float32 with -10 where rejected, R as float32)."""
+        S = self.sgm(self.ad_census(center, other, D))
+        L = self.median_inplace(self.wta(S, right=False))
+        R = self.median_inplace(self.wta(S, right=True))
+        return self.lrcheck(L, R), R
 
     def compute(self, views, dc, modes=(True, True, True)):
         h, w = views[0].shape

@@ -393,6 +393,66 @@ void orc_wta_left_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp) 
     }
 }
 
+/* WTARight_SSE(disp, vol, W, H, D-1, 1) (postprocess.cpp:187-315): R(j) = the lowest k <= min(D-1, W-1-j)
+   minimising vol(i, j+k, k). Both of its branches keep the lowest index (the SSE search replaces the running
+   minimum only on a strictly smaller block minimum, _mm_minpos_epu16 returns the lowest index of a block, the
+   border loop compares strictly), and uniqueness 1 never rejects (1024 * min <= 1024 * second minimum). */
+void orc_wta_right_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < H; i++) {
+        for (int j = 0; j < W; j++) {
+            const int end = (W - 1 - j) < (D - 1) ? (W - 1 - j) : (D - 1);
+            int best = 0;
+            uint16_t bc = vol[((size_t)i * W + j) * D];
+            for (int k = 1; k <= end; k++) {
+                const uint16_t c = vol[((size_t)i * W + j + k) * D + k];
+                if (c < bc) { bc = c; best = k; }
+            }
+            disp[(size_t)i * W + j] = (uint16_t)best;
+        }
+    }
+}
+
+/* doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) on integer maps: L(i, j) is kept where 0 <= L <= j and
+   |L - R(i, j - L)| <= 5, else it becomes -10. */
+void orc_lrcheck(const uint16_t *L, const uint16_t *R, int W, int H, int16_t *out) {
+    for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+            const int b = L[(size_t)i * W + j];
+            int keep = 0;
+            if (b <= j) {
+                const int diff = b - (int)R[(size_t)i * W + j - b];
+                keep = diff <= 5 && diff >= -5;
+            }
+            out[(size_t)i * W + j] = keep ? (int16_t)b : (int16_t)-10;
+        }
+}
+
+/* doStereo (SisterMultiviewDisparities.hpp:122-150): ad_census -> sgm -> WTALeft / WTARight -> in-place medians
+   -> doLRCheck, on unpadded w x h images. L gets -10 where the LR check rejects; R is the median-filtered right map.
+   Returns 0, or -1 when memory runs out. */
+int orc_stereo(const uint8_t *center, const uint8_t *other, int w, int h, int D, int16_t *L_out, uint16_t *R_out) {
+    const size_t plane = (size_t)w * h;
+    uint64_t *cc = (uint64_t *)malloc(plane * 8), *cn = (uint64_t *)malloc(plane * 8);
+    uint16_t *vol = (uint16_t *)malloc(plane * D * 2), *S = (uint16_t *)malloc(plane * D * 2);
+    uint16_t *L = (uint16_t *)malloc(plane * 2);
+    int rc = -1;
+    if (cc && cn && vol && S && L) {
+        orc_census(center, w, h, cc);
+        orc_census(other, w, h, cn);
+        orc_cost_volume(cc, cn, w, h, D, vol);
+        orc_sgm(vol, w, h, D, S);
+        orc_wta_left_vol(S, w, h, D, L);
+        orc_wta_right_vol(S, w, h, D, R_out);
+        orc_median_inplace(L, w, h);
+        orc_median_inplace(R_out, w, h);
+        orc_lrcheck(L, R_out, w, h, L_out);
+        rc = 0;
+    }
+    free(cc); free(cn); free(vol); free(S); free(L);
+    return rc;
+}
+
 /* convertTo(CV_16UC1), ROI Rect(dc, dc, Wp-2dc, Hp-2dc), then * 255 with u16 saturation (hpp:111-118). */
 void orc_crop_scale(const uint16_t *disp, int Wp, int dc, int w, int h, uint16_t *out) {
     for (int i = 0; i < h; i++)

@@ -62,6 +62,9 @@ void orc_sgm_passes(const uint16_t *C, int W, int H, int D, uint16_t *S, int npa
 
 /* WTA-left (argmin over d<=min(j,D-1), lowest d on ties) of a volume. */
 void orc_wta_left_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp);
+void orc_wta_right_vol(const uint16_t *vol, int W, int H, int D, uint16_t *disp);
+void orc_lrcheck(const uint16_t *L, const uint16_t *R, int W, int H, int16_t *out);
+int orc_stereo(const uint8_t *center, const uint8_t *other, int w, int h, int D, int16_t *L_out, uint16_t *R_out);
 
 /* Crop [dc,dc+h)x[dc,dc+w) and scale by 255 with u16 saturation (hpp:111-118). */
 void orc_crop_scale(const uint16_t *disp, int Wp, int dc, int w, int h, uint16_t *out);

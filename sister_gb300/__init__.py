@@ -67,6 +67,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.sister_set_max_disparity.argtypes = [_vp, ctypes.c_int]
     lib.sister_compute.argtypes = [_vp, _vp, _vp, _vp]
     lib.sister_compute_device.argtypes = [_vp, _vp, _vp, _vp]
+    lib.sister_stereo.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]
     lib.sister_set_stream.argtypes = [_vp, _vp]
     lib.sister_synchronize.argtypes = [_vp]
     lib.sister_device_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -173,6 +174,20 @@ class Context:
         ptrs = [o.ctypes.data if o is not None else None for o in outs]
         self._check(self.lib.sister_compute(self.h, *ptrs))
         return outs
+
+    def stereo(self, center, other, dc: int):
+        """Two-view doStereo (SisterMultiviewDisparities.hpp:122-150) on one gray image pair: returns (left int16,
+        -10 where the LR check rejects; right uint16, the median-filtered right map)."""
+        a = np.ascontiguousarray(center, np.uint8)
+        b = np.ascontiguousarray(other, np.uint8)
+        if a.shape != b.shape or a.ndim != 2:
+            raise ValueError("stereo: center and other must be 2-D gray images of the same shape")
+        h, w = a.shape
+        left = np.empty((h, w), np.int16)
+        right = np.empty((h, w), np.uint16)
+        self._check(self.lib.sister_stereo(self.h, a.ctypes.data, b.ctypes.data, w, h, w, int(dc), left.ctypes.data,
+                                           right.ctypes.data))
+        return left, right
 
     def compute_device(self, multi_ptr=None, horiz_ptr=None, vert_ptr=None):
         self._check(self.lib.sister_compute_device(self.h, multi_ptr, horiz_ptr, vert_ptr))

@@ -8,7 +8,8 @@ namespace {
 //   M(d) = sum over used frames f of mask_f(i, j) * C_f(a_f, b_f, d)
 // where (a_f, b_f) are the frame coordinates of (i, j) (hpp:259-261) and C_f is the pair's Hamming cell
 // of census.cpp:54-146: 255 for frame rows 0..2, 0 for the two last rows (never written there), 255 for
-// d > b, else popcount(Cc[a][b] ^ Cn[a][b-d]). Mode 0 uses all frames, 1 frames {0,2}, 2 frames {1,3}.
+// d > b, else popcount(Cc[a][b] ^ Cn[a][b-d]). Mode 0 uses all frames, 1 frames {0,2}, 2 frames {1,3}; mode 3 is the
+// two-view doStereo volume (ad_census of hpp:135): frame 0 alone, without mask (masks may be null).
 // The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
 // (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
 // One warp per pixel, lanes over d (lane l holds d = l + 32k, k < DPL); 8 pixels of one row per CTA. The
@@ -28,8 +29,8 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     for (int k = 0; k < DPL; k++) acc[k] = 0;
 #pragma unroll
     for (int f = 0; f < 4; f++) {
-        const bool in_mode = (mode == 0) || (mode == 1 && !(f & 1)) || (mode == 2 && (f & 1));
-        if (!in_mode || !masks[(size_t)f * g.plane + p]) continue; // warp-uniform
+        const bool in_mode = (mode == 0) || (mode == 1 && !(f & 1)) || (mode == 2 && (f & 1)) || (mode == 3 && f == 0);
+        if (!in_mode || (mode != 3 && !masks[(size_t)f * g.plane + p])) continue; // warp-uniform
         int fa, fb;
         switch (f) {
         case 0: fa = i; fb = j; break;

@@ -356,6 +356,25 @@ __global__ void lrc_mask_kernel(const uint16_t *__restrict__ med, Geom g, uint8_
     masks[(size_t)f * g.plane + (size_t)i * g.Wp + j] = m;
 }
 
+// doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) as the two-view doStereo applies it (hpp:145): the left map
+// keeps L where 0 <= L <= j and |L - R[j-L]| <= 5 and becomes -10 elsewhere; the right map is passed through.
+// med holds the median-filtered maps of frame 0 (L, then R).
+__global__ void stereo_lrc_kernel(const uint16_t *__restrict__ med, Geom g, int16_t *__restrict__ outL,
+                                  uint16_t *__restrict__ outR) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= g.Wp || i >= g.Hp) return;
+    const size_t p = (size_t)i * g.Wp + j;
+    const uint16_t *L = med, *R = med + g.plane;
+    const int base = L[p];
+    bool keep = false;
+    if (base <= j) {
+        const int diff = base - (int)R[p - base];
+        keep = diff <= 5 && diff >= -5;
+    }
+    outL[p] = keep ? (int16_t)base : (int16_t)-10;
+    outR[p] = R[p];
+}
+
 } // namespace
 
 void init_mask_kernels() {
@@ -398,6 +417,10 @@ void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uin
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
                                                                                        epoch, err);
+}
+
+void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16_t *outR, cudaStream_t st) {
+    stereo_lrc_kernel<<<dim3((g.Wp + 255) / 256, g.Hp), 256, 0, st>>>(med, g, outL, outR);
 }
 
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {

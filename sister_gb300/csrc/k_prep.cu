@@ -154,9 +154,9 @@ void launch_frames(const uint8_t *views_dev, const Geom &g, uint8_t *frames, cud
     frames_kernel<<<grid, dim3(32, 8), 0, st>>>(views_dev, g, frames);
 }
 
-void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st) {
+void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st, int nimg) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    dim3 grid((mx + 31) / 32, (mx + 7) / 8, 8);
+    dim3 grid((mx + 31) / 32, (mx + 7) / 8, nimg);
     census_kernel<<<grid, dim3(32, 8), 0, st>>>(frames, g, census);
 }
 

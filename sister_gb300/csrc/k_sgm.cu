@@ -618,6 +618,31 @@ __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict
     }
 }
 
+// WTARight_SSE with uniqueness 1 (postprocess.cpp:187-315) on S0 + S1, for the two-view doStereo (hpp:139):
+// R(i, b) = the lowest k <= min(dc-1, W-1-b) minimising S(i, b+k, k). One warp per pixel, lanes over k; the cells
+// lie on a diagonal of the volume (stride dp + 1), which only this path reads.
+template <int DPL>
+__global__ void __launch_bounds__(256) sgm_wta_right_kernel(const uint16_t *__restrict__ s0v,
+                                                            const uint16_t *__restrict__ s1v, Geom g,
+                                                            uint16_t *__restrict__ disp) {
+    const int lane = threadIdx.x & 31;
+    const size_t pix = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (pix >= g.plane) return;
+    const int b = (int)(pix % g.Wp);
+    const int end = min(g.dc - 1, g.Wp - 1 - b);
+    uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+    for (int t = 0; t < DPL; t++) {
+        const int k = lane * DPL + t;
+        if (k <= end) {
+            const size_t cell = (pix + k) * g.dp + k;
+            best = min(best, ((uint32_t)(s0v[cell] + s1v[cell]) << 16) | (uint32_t)k);
+        }
+    }
+    best = __reduce_min_sync(FULL, best);
+    if (lane == 0) disp[pix] = (uint16_t)(best & 0xFFFFu);
+}
+
 const void *kernel_for(int dpl) {
     switch (dpl) {
     case 2: return (const void *)sgm_kernel<2>;
@@ -785,6 +810,21 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
     void *args[] = {(void *)&a};
     return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R + kHelpers) * 32), args,
                                        sgm_smem(R, dp).total, st);
+}
+
+cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,
+                                 cudaStream_t st) {
+    const unsigned blocks = (unsigned)((g.plane + 7) / 8);
+    switch (g.dpl) {
+    case 2: sgm_wta_right_kernel<2><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    case 4: sgm_wta_right_kernel<4><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    case 6: sgm_wta_right_kernel<6><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    case 8: sgm_wta_right_kernel<8><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    case 12: sgm_wta_right_kernel<12><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    case 16: sgm_wta_right_kernel<16><<<blocks, 256, 0, st>>>(s0, s1, g, disp); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *out, uint16_t *disp,

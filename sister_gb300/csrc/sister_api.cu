@@ -367,6 +367,85 @@ int sister_compute(sister_ctx *c, uint16_t *multi, uint16_t *horiz, uint16_t *ve
     return read_device_error(c);
 }
 
+int sister_stereo(sister_ctx *c, const uint8_t *center, const uint8_t *other, int width, int height, int stride,
+                  int dc, int16_t *left, uint16_t *right) {
+    if (!c) return SISTER_EINVAL;
+    if (!center || !other || !left || !right) return c->fail(SISTER_EINVAL, "stereo: NULL image or output");
+    int rc = check_geometry(c, width, height, dc);
+    if (rc) return rc;
+    if (stride < width) return c->fail(SISTER_EINVAL, "stride %d < width", stride);
+    cudaSetDevice(c->device);
+    // doStereo works on the images as given (no padding): frame 0 of a geometry whose padded size is the image
+    Geom g{};
+    g.w = width;
+    g.h = height;
+    g.dc = dc;
+    g.Wp = width;
+    g.Hp = height;
+    g.dpl = choose_dpl(dc);
+    g.dp = 32 * g.dpl;
+    g.plane = (size_t)width * height;
+    const SgmPlan p = sgm_plan(g, c->device);
+    if (p.R < 1) return c->fail(SISTER_EDEVICE, "no launch configuration fits the aggregation kernel");
+    const size_t plane = g.plane, vol = plane * g.dp;
+    struct {
+        DevBuf *b;
+        size_t bytes;
+        const char *what;
+    } req[] = {
+        {&c->frames, 2 * plane, "frames"},
+        {&c->census, 2 * plane * sizeof(uint64_t), "census"},
+        {&c->wta, 2 * plane * sizeof(uint16_t), "wta"},
+        {&c->med, 2 * plane * sizeof(uint16_t), "median"},
+        {&c->cost, vol * sizeof(uint16_t), "cost volume"},
+        {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
+        {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
+        {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
+        {&c->progress, progress_bytes(std::max(p.ngroups, 1)), "progress"},
+        {&c->outs, 2 * plane * sizeof(uint16_t), "outputs"},
+    };
+    for (auto &r : req) {
+        cudaError_t e = r.b->ensure(r.bytes);
+        if (e != cudaSuccess) return c->cuda_fail(e, r.what);
+    }
+    c->have_intermediates = false; // the multiview intermediates are overwritten
+    cudaStream_t st = c->stream;
+    uint8_t *frames = c->frames.as<uint8_t>();
+    cudaError_t e = cudaMemsetAsync(c->errflag.p, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(frames, width, center, stride, width, height, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(frames + plane, width, other, stride, width, height, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "copying images");
+    // ad_census (hpp:135): census of both images, Hamming volume (frame 0 alone, unmasked)
+    launch_census(frames, g, c->census.as<uint64_t>(), st, 2);
+    launch_masked_cost(c->census.as<uint64_t>(), nullptr, g, 3, c->cost.as<uint16_t>(), st);
+    // sgm (hpp:138)
+    SgmRig a{};
+    a.cost = c->cost.as<uint16_t>();
+    a.sum0 = c->sum0.as<uint16_t>();
+    a.sum1 = c->sum1.as<uint16_t>();
+    a.bnd = c->bnd.as<uint16_t>();
+    a.progress = c->progress.as<unsigned>();
+    e = launch_sgm(g, p, a, c->errflag.as<unsigned>(), st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
+    // WTALeft / WTARight (hpp:141-142) into maps 0 and 1 of frame 0, their in-place medians (hpp:143-144), LR check
+    uint16_t *wta = c->wta.as<uint16_t>();
+    e = launch_sgm_wta(g, a.sum0, a.sum1, nullptr, wta, st);
+    if (e == cudaSuccess) e = launch_sgm_wta_right(g, a.sum0, a.sum1, wta + plane, st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
+    launch_median(wta, g, c->med.as<uint16_t>(), st, 0, 1);
+    int16_t *dl = c->outs.as<int16_t>();
+    uint16_t *dr = c->outs.as<uint16_t>() + plane;
+    launch_stereo_lrc(c->med.as<uint16_t>(), g, dl, dr, st);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(left, dl, plane * sizeof(int16_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(right, dr, plane * sizeof(uint16_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "stereo");
+    return read_device_error(c);
+}
+
 int sister_set_stream(sister_ctx *c, void *stream) {
     if (!c) return SISTER_EINVAL;
     c->stream = stream ? (cudaStream_t)stream : c->own_stream;

@@ -73,7 +73,8 @@ void init_sgm_kernels();
 void launch_to_gray(const uint8_t *const src[5], int stride, int channels, int w, int h, uint8_t *views_dev,
                     cudaStream_t st);
 void launch_frames(const uint8_t *views_dev, const Geom &g, uint8_t *frames, cudaStream_t st);
-void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st);
+// census of the first nimg frame images (8: all four frame pairs; 2: frame 0 only)
+void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaStream_t st, int nimg = 8);
 // the mask stages run on frames [f0, f0 + nf) (all four by default)
 // rowflags (4 x max(Wp, Hp) u32, or null): pair WTA publishes each frame row with `epoch`; a median given the
 // same flags waits for the rows it reads, so it may be launched before the frame's pair WTA has finished.
@@ -84,6 +85,8 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
 // pair WTA of every frame and the eight medians in one launch (medians follow the rows through rowflags)
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
                        unsigned epoch, unsigned *err, cudaStream_t st);
+// two-view doStereo tail: LR-checked left map (-10 where rejected) and the right map, from frame 0's medians
+void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16_t *outR, cudaStream_t st);
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st);
@@ -102,6 +105,9 @@ int sgm_rows_gb300(int dp); // sgm_rows_max on a GB300, without a device query
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
                              unsigned *err, int device, cudaStream_t st);
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
+// WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
+cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,
+                                 cudaStream_t st);
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *sum0, const uint16_t *sum1, uint16_t *out, uint16_t *disp,
                            cudaStream_t st);
 

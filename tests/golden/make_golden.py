@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures from the reference's own compiled code (oracle/_ref).
 
 Run from the repository root on an x86-64 host that has the reference tree:
-    python tests/golden/make_golden.py [--c2]
+    python tests/golden/make_golden.py [--c2] [--stereo-only]
 
 Every case stores the SHA-256 of its five input views (so a test first checks that the seeded
 generator reproduces the same bytes on the machine it runs on) and the reference outputs of the three
@@ -50,9 +50,33 @@ def small_cases():
     return cases
 
 
+def stereo_cases():
+    """(name, center, other, dc) for the two-view doStereo fixtures: random pairs and synthetic center/right pairs."""
+    rng = np.random.default_rng(20241203)
+    cases = []
+    for (h, w, dc) in [(16, 24, 8), (32, 48, 16)]:
+        cases.append(("stereo_rand_%dx%d_dc%d" % (w, h, dc), rng.integers(0, 256, (h, w), dtype=np.uint8),
+                      rng.integers(0, 256, (h, w), dtype=np.uint8), dc))
+    for k, (w, h, dc) in enumerate([(96, 64, 24), (160, 120, 48), (200, 148, 64)]):
+        views, _ = synth.make_rig(w, h, 2, dc - 8, seed=300 + k, tiles=4)
+        cases.append(("stereo_synth_%dx%d_dc%d" % (w, h, dc), views[0], views[1], dc))
+    return cases
+
+
+def make_stereo(ref):
+    for name, center, other, dc in stereo_cases():
+        L, R = ref.stereo(center, other, dc)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), center=center, other=other, dc=dc,
+                            left=L.astype(np.int16), right=R.astype(np.uint16))
+        print(name)
+
+
 def main():
     ref = oracle.Ref()
     t0 = time.time()
+    make_stereo(ref)
+    if "--stereo-only" in sys.argv:
+        return
     for name, views, dc in small_cases():
         multi, horiz, vert = ref.compute(views, dc)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), views=np.stack(views), dc=dc, multi=multi,
