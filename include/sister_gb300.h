@@ -132,7 +132,9 @@ enum {
     SISTER_TUNE_SGM_ROWS = 1,     /* image rows per CTA (one warp each); 0 = automatic */
     SISTER_TUNE_SGM_CLUSTER = 2,  /* CTAs per thread-block cluster (1, 2, 4 or 8); 0 = automatic */
     SISTER_TUNE_SGM_GROUPS = 3,   /* read-only: cluster-sized row groups of the current geometry */
-    SISTER_TUNE_SGM_CLUSTERS = 4  /* read-only: co-resident clusters launched */
+    SISTER_TUNE_SGM_CLUSTERS = 4, /* read-only: co-resident clusters launched */
+    SISTER_TUNE_FULL_DISP = 5     /* 1: also write the padded winner-take-all map (SISTER_DBG_DISP); 0 (default):
+                                     only the cropped outputs are computed */
 };
 /* Set a knob for subsequent computes (no reference counterpart: the reference is single-threaded CPU code). */
 SISTER_API int sister_tune_set(sister_ctx *ctx, int key, int value);
@@ -195,7 +197,7 @@ enum {
     SISTER_DBG_MASKS = 5,  /* index f: confidence mask of frame f in padded original coordinates (u8) */
     SISTER_DBG_COST = 6,   /* index 0: masked multiview cost of the last aggregated mode (u16, d stride dp) */
     SISTER_DBG_SUM0 = 7,   /* index 0: pass-0 SGM sum of the last aggregated mode (u16, d stride dp) */
-    SISTER_DBG_DISP = 8,   /* index mode: padded winner-take-all disparity (u16, Hp x Wp) */
+    SISTER_DBG_DISP = 8,   /* index mode: padded winner-take-all disparity (u16, Hp x Wp); needs SISTER_TUNE_FULL_DISP = 1 */
     SISTER_DBG_DP = 9      /* returns the padded disparity stride dp of the volumes in *(int*)dst */
 };
 SISTER_API int sister_debug_fetch(sister_ctx *ctx, int what, int index, void *host_dst, size_t bytes);

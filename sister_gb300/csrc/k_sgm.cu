@@ -585,16 +585,26 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
 
 // Sum of the two passes' sums and the final WTALeft (hpp:283, postprocess.cpp:74-185): the lowest
 // d <= min(j, dc-1) of S0 + S1 (pass 1 adds its sum to pass 0's, saturating at sgm.cpp:390 -- real sums
-// stay below 2 * 4 * 1121, so nothing saturates), then crop and *255 (hpp:111-118). One warp per padded
-// pixel, lanes over d; memory-bound (reads both sum volumes once).
+// stay below 2 * 4 * 1121, so nothing saturates), then crop and *255 (hpp:111-118). One warp per pixel, lanes
+// over d; memory-bound. Without a padded map to fill (disp null) only the cropped pixels are computed, which
+// reads the sum volumes over w*h pixels instead of Wp*Hp.
 template <int DPL>
 __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict__ s0v, const uint16_t *__restrict__ s1v,
                                                       Geom g, uint16_t *__restrict__ out, uint16_t *__restrict__ disp) {
     constexpr int NP = DPL / 2;
     const int lane = threadIdx.x & 31;
-    const size_t pix = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (pix >= g.plane) return;
-    const int i = (int)(pix / g.Wp), j = (int)(pix % g.Wp);
+    const size_t t = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int i, j;
+    if (disp) {
+        if (t >= g.plane) return;
+        i = (int)(t / g.Wp);
+        j = (int)(t % g.Wp);
+    } else {
+        if (t >= (size_t)g.w * g.h) return;
+        i = (int)(t / g.w) + g.dc;
+        j = (int)(t % g.w) + g.dc;
+    }
+    const size_t pix = (size_t)i * g.Wp + j;
     const int d0 = lane * DPL, D = g.dc;
     uint32_t s0[NP], s1[NP];
     ldw<NP>(s0v + pix * g.dp + d0, s0);
@@ -829,7 +839,7 @@ cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16
 
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *out, uint16_t *disp,
                            cudaStream_t st) {
-    const unsigned blocks = (unsigned)((g.plane + 7) / 8);
+    const unsigned blocks = (unsigned)(((disp ? g.plane : (size_t)g.w * g.h) + 7) / 8);
     switch (g.dpl) {
     case 2: sgm_wta_kernel<2><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
     case 4: sgm_wta_kernel<4><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;

@@ -68,6 +68,7 @@ struct sister_ctx {
     SgmPlan plan{};
     int plan_w = 0, plan_h = 0, plan_dc = 0;
     int tune_rows = 0, tune_cs = 0;
+    bool full_disp = false; // keep the padded disparity map (debug inspection)
     // stage profiling: events recorded on the context stream around every stage of a compute
     bool prof = false;
     std::vector<cudaEvent_t> ev;
@@ -250,7 +251,8 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->mark(SISTER_STAGE_AGGREGATE);
-        e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode], c->disp.as<uint16_t>() + (size_t)mode * g.plane, st);
+        e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode],
+                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)mode * g.plane : nullptr, st);
         if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
         c->mark(SISTER_STAGE_WTA);
         c->last_mode = mode;
@@ -522,6 +524,7 @@ int sister_tune_set(sister_ctx *c, int key, int value) {
             return c->fail(SISTER_EINVAL, "cluster size must be 0, 1, 2, 4 or 8");
         c->tune_cs = value;
         break;
+    case SISTER_TUNE_FULL_DISP: c->full_disp = value != 0; return SISTER_OK;
     default: return c->fail(SISTER_EINVAL, "unknown or read-only tuning key %d", key);
     }
     c->plan_w = c->plan_h = c->plan_dc = 0; // re-plan on next use
@@ -538,6 +541,7 @@ int sister_tune_get(sister_ctx *c, int key, int *value) {
     case SISTER_TUNE_SGM_CLUSTER: *value = p.cs; break;
     case SISTER_TUNE_SGM_GROUPS: *value = p.ngroups; break;
     case SISTER_TUNE_SGM_CLUSTERS: *value = p.nclusters; break;
+    case SISTER_TUNE_FULL_DISP: *value = c->full_disp ? 1 : 0; break;
     default: return c->fail(SISTER_EINVAL, "unknown tuning key %d", key);
     }
     return SISTER_OK;
@@ -564,7 +568,11 @@ int sister_debug_fetch(sister_ctx *c, int what, int index, void *dst, size_t byt
     case SISTER_DBG_MASKS: src = c->masks.as<char>() + (size_t)index * plane; need = plane; break;
     case SISTER_DBG_COST: src = c->cost.as<char>(); need = plane * g.dp * 2; break;
     case SISTER_DBG_SUM0: src = c->sum0.as<char>(); need = plane * g.dp * 2; break;
-    case SISTER_DBG_DISP: src = c->disp.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
+    case SISTER_DBG_DISP:
+        if (!c->full_disp) return c->fail(SISTER_ESTATE, "the padded disparity map is kept only with SISTER_TUNE_FULL_DISP = 1");
+        src = c->disp.as<char>() + (size_t)index * plane * 2;
+        need = plane * 2;
+        break;
     default: return c->fail(SISTER_EINVAL, "unknown debug item %d", what);
     }
     if (index < 0 || index > 7 || bytes < need) return c->fail(SISTER_EINVAL, "bad debug index/size");

@@ -108,6 +108,7 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,
                                  cudaStream_t st);
+// disp (padded Hp x Wp map) may be null: then only the cropped output pixels are computed
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *sum0, const uint16_t *sum1, uint16_t *out, uint16_t *disp,
                            cudaStream_t st);
 

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def ctx(gpu_lib):
     c = sg.Context(0)
+    c.tune_set(sg.TUNE_FULL_DISP, 1)  # keep the padded winner-take-all map for the stage checks
     yield c
     c.close()
 
@@ -185,3 +186,21 @@ def test_errors(ctx):
         c.load_views([np.zeros((30, 40), np.uint8)] * 5)
     assert e.value.code == -1
     c.close()
+
+
+def test_full_disp_switch(gpu_lib):
+    """The padded map is only kept on request; the outputs are the same either way."""
+    views, _ = synth.make_rig(96, 64, 2, 20, seed=9, tiles=4)
+    c = sg.Context(0)
+    c.load_views(views)
+    c.set_max_disparity(24)
+    crop_only = c.compute(True, True, True)
+    with pytest.raises(sg.SisterError):
+        c.debug(sg.DBG_DISP, 0, (64 + 48, 96 + 48), np.uint16)
+    c.tune_set(sg.TUNE_FULL_DISP, 1)
+    full = c.compute(True, True, True)
+    disp = c.debug(sg.DBG_DISP, 0, (64 + 48, 96 + 48), np.uint16)
+    c.close()
+    for a, b in zip(crop_only, full):
+        assert np.array_equal(a, b)
+    assert np.array_equal(full[0].astype(np.int64), np.minimum(disp[24:88, 24:120].astype(np.int64) * 255, 65535))

@@ -24,6 +24,7 @@ def test_stress_rig_4096x3000_dc512(gpu_lib):
         pytest.skip("needs %.0f GB of device memory, %.0f GB free" % (need / 2**30, free / 2**30))
     (views, gt), dc = synth.rig_c5(5)
     ctx = sg.Context(0)
+    ctx.tune_set(sg.TUNE_FULL_DISP, 1)
     ctx.load_views(views)
     ctx.set_max_disparity(dc)
     multi = ctx.compute(True, False, False)[0]

@@ -27,6 +27,7 @@ def test_static_entry_matches_compute(gpu_lib):
     w, h, dc = 128, 96, 40
     views, _ = synth.make_rig(w, h, 2, 32, seed=31, tiles=4)
     ctx = sg.Context(0)
+    ctx.tune_set(sg.TUNE_FULL_DISP, 1)
     ctx.load_views(views)
     ctx.set_max_disparity(dc)
     multi = ctx.compute(True, False, False)[0]           # existing entry point
