@@ -12,7 +12,8 @@ namespace {
 // two-view doStereo volume (ad_census of hpp:135): frame 0 alone, without mask (masks may be null).
 // The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
 // (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
-// One warp per pixel, lanes over d (lane l holds d = l + 32k, k < DPL); 8 pixels of one row per CTA. The
+// One warp per pixel, lanes over d (lane l holds d = l + 32k, k < DPL); 8 pixels of one row per CTA, CTAs ordered
+// row-fastest. The
 // frame loop is outside the d loop so that the DPL census loads of one frame are independent and issue
 // back to back (the transposed frames' words come from L2).
 template <int DPL>
@@ -20,7 +21,7 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
                                                           uint16_t *__restrict__ cost) {
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int i = blockIdx.y, j = blockIdx.x * 8 + wp;
+    const int i = blockIdx.x, j = blockIdx.y * 8 + wp;
     if (j >= g.Wp) return;
     const size_t p = (size_t)i * g.Wp + j;
     const int D = g.dc;
@@ -71,7 +72,9 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
 
 void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                         cudaStream_t st) {
-    dim3 grid((g.Wp + 7) / 8, g.Hp);
+    // rows fastest: consecutive CTAs share the transposed frames' census rows (a frame-1/3 row is a padded
+    // column), which then come from L1/L2 instead of being gathered again
+    dim3 grid(g.Hp, (g.Wp + 7) / 8);
     switch (g.dpl) {
     case 2: masked_cost_kernel<2><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
     case 4: masked_cost_kernel<4><<<grid, 256, 0, st>>>(census, masks, g, mode, cost); break;
