@@ -115,6 +115,23 @@ def dist_env():
     return rank, local, world
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest of every rank's x (all ranks get it): the step time of a replica run is the slowest rank's."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, steps: int, units_per_rig: float, seconds: float) -> float:
+    """Whole-job throughput of N replicas: every rank computes `steps` rigs; the job takes the slowest rank's time."""
+    return world * steps * units_per_rig / seconds
+
+
 def make_rig():
     from sister_gb300 import synth
 
@@ -343,12 +360,8 @@ def run_gb300(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ctx.profile(False)
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * rig_units() / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world)
+    value = replica_value(world, args.steps, rig_units(), total_ms / 1e3)
 
     # end to end through the public API: pinned host views in, pinned host disparity out, every step
     pin_views = [torch.from_numpy(v).pin_memory() for v in views]
@@ -363,11 +376,7 @@ def run_gb300(args):
     for _ in range(args.steps):
         ctx.load_views_host(ptrs, w, h, w, 1)
         ctx.compute_host(pin_out.data_ptr())
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_ok = bool((pin_out.numpy().view(np.uint16) == got).all())
 
     # roofline of the dominant kernel (the aggregation launch, both passes): algorithmic bytes per launch =
@@ -392,7 +401,7 @@ def run_gb300(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": CONFIG,
             "impl": "gb300", "bit_exact_vs_reference_golden": bit_exact,
-            "e2e": {"value": world * args.steps * rig_units() / e2e_s, "unit": UNIT,
+            "e2e": {"value": replica_value(world, args.steps, rig_units(), e2e_s), "unit": UNIT,
                     "h2d_bytes_per_step": 5 * w * h, "d2h_bytes_per_step": 2 * w * h, "output_matches": e2e_ok},
             "gpu_launches": KERNELS_PER_COMPUTE * args.steps,
             "stage_ms_mean": {k: sum(v) / len(v) for k, v in stage_ms.items()},
