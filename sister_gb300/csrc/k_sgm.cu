@@ -27,10 +27,12 @@
 //     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows of FB
 //     consecutive pixels per copy into a two-group ring per row, one group ahead;
 //   * the last row of a band is handed to the next band through global memory: its ring (kKS slots) is
-//     read by a writer warp that stores the records and, at the end of every hand-off batch (2, 2, 4
-//     pixels, then FB at a time), fences and releases a progress counter. A fetcher warp of the next band
-//     polls that counter and bulk-copies each batch of records into a ring of 2*FB slots for its first
-//     row, so a band starts two pixels after the one above. Row warps never fence or poll global memory.
+//     read by a writer warp that stores the records and, at the end of every 2-pixel hand-off batch,
+//     publishes its count in shared memory; a releaser warp turns the latest count into a device-scope
+//     release of the band's progress counter, so the writer never waits on a device-wide fence (about a
+//     microsecond each, longer than two pixel periods). A fetcher warp of the next band polls that counter
+//     and bulk-copies each batch of records into a ring of 2*FB slots for its first row, so a band starts
+//     two pixels after the one above. Row warps never fence or poll global memory.
 // Arithmetic is packed u16x2: minima with __vminu2, additions and subtractions as plain 32-bit IADDs, which
 // equal packed u16x2 ones whenever no half carries or borrows. That holds on the recurrence: a path value is
 // C + (m - minLp) with minLp <= m <= minLp + 100, so real entries stay below 1021 + 100 and "infinite"
@@ -46,13 +48,18 @@
 
 namespace sister {
 
-constexpr int kHelpers = 2; // fetcher and writer warps
+constexpr int kHelpers = 3; // fetcher, writer and releaser warps
 constexpr int kKP = 4;      // ring slots of a row read by the row below
 constexpr int kKS = 8;      // ring slots of the band's last row, read by the writer
 // most rows per band (one warp each) by d-stride; shared memory may allow fewer
 __host__ __device__ constexpr int rows_cap(int dp) { return dp <= 256 ? 14 : dp <= 384 ? 12 : 9; }
 // pixels per batched copy: cost group of a row, and records per fetch
 __host__ __device__ constexpr int batch_px(int dp) { return dp >= 384 ? 4 : 8; }
+// pixels per hand-off batch between bands (batches of 2 measured fastest once the device-wide release moved off
+// the writer: 4.48 ms against 4.61 for 4 and 4.54 for 8 on 1920x1080/256), and the number of such batches the
+// incoming ring (2 * batch_px slots) holds, each with its own full barrier
+__host__ __device__ constexpr int hand_px(int) { return 2; }
+__host__ __device__ constexpr int in_batches(int dp) { return 2 * batch_px(dp) / hand_px(dp); }
 
 // one pixel's record, in ring slots and in the global hand-off rows alike: r1 | r2 | r3 (dp u16 each) |
 // minima m1 m2 m3 (+5 pad)
@@ -64,15 +71,16 @@ struct SgmSmem {
 };
 // ring slots: row w < R-1 owns slots [w*kKP, w*kKP + kKP), row R-1 owns [(R-1)*kKP, (R-1)*kKP + kKS)
 // barriers (8 bytes each; FB = batch_px(dp), KI = 2*FB): slot k full at 2k, empty at 2k+1; then the incoming
-// ring's batch full barriers [2] and per-slot empty barriers [KI]; then cost group g (0, 1) of row w at 2w + g
+// ring's batch full barriers [in_batches] and per-slot empty barriers [KI]; then cost group g (0, 1) of row w at
+// 2w + g
 __host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
     SgmSmem L{};
     const int FB = batch_px(dp), KI = 2 * FB;
     L.nslot = (R - 1) * kKP + kKS;
-    L.nbar = 2 * L.nslot + 2 + KI + 2 * R;
+    L.nbar = 2 * L.nslot + in_batches(dp) + KI + 2 * R;
     size_t o = 0;
     L.bars = o;
-    o += (size_t)L.nbar * 8;
+    o += (size_t)L.nbar * 8 + 8; // + the writer's count of records copied to global memory (u32)
     o = (o + 127) & ~(size_t)127;
     L.rings = o;
     o += (size_t)L.nslot * rec_u16(dp) * 2;
@@ -145,6 +153,14 @@ __device__ __forceinline__ bool mbar_sleep(uint32_t a, uint32_t par, uint32_t ns
                  : "r"(a), "r"(par), "r"(ns)
                  : "memory");
     return ok != 0;
+}
+__device__ __forceinline__ void st_release_cta_shared(uint32_t a, unsigned v) {
+    asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_cta_shared(uint32_t a) {
+    unsigned v;
+    asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
 }
 __device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
     unsigned v;
@@ -263,6 +279,8 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     constexpr int NP = DPL / 2;
     constexpr int FB = batch_px(32 * DPL); // pixels per cost copy
     constexpr int KI = 2 * FB;             // incoming-ring slots
+    constexpr int HB = hand_px(32 * DPL);  // pixels per full hand-off batch
+    constexpr int NIB = in_batches(32 * DPL);
     extern __shared__ __align__(128) unsigned char smem[];
     const int R = a.R, dp = a.dp;
     int W = 0, H = 0; // geometry of the current work item's rig
@@ -271,12 +289,13 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     const int rec = rec_u16(dp);
     const SgmSmem L = sgm_smem(R, dp);
     const uint32_t bars = sptr(smem + L.bars);
+    const uint32_t relcnt = bars + 8u * (uint32_t)L.nbar; // records of this band copied to global memory
     // ring of row w: kKP slots (kKS for the last row); slot k's full barrier at bars + 16k, empty at +8
     auto lgslots = [&](int w) { return w == R - 1 ? 3 : 2; };
     const uint32_t in_base = bars + 16u * (uint32_t)L.nslot;
-    auto infull = [&](int b) { return in_base + 8u * (uint32_t)(b & 1); };         // batch b
-    auto inempty = [&](int x) { return in_base + 16u + 8u * (uint32_t)(x & (KI - 1)); }; // pixel x's slot
-    const uint32_t c_base = in_base + 16u + 8u * (uint32_t)KI;
+    auto infull = [&](int b) { return in_base + 8u * (uint32_t)(b & (NIB - 1)); };              // batch b
+    auto inempty = [&](int x) { return in_base + 8u * (uint32_t)(NIB + (x & (KI - 1))); };      // pixel x's slot
+    const uint32_t c_base = in_base + 8u * (uint32_t)(NIB + KI);
     auto cfull = [&](int w, int g) { return c_base + 8u * (uint32_t)(w * 2 + (g & 1)); };
     uint16_t *rings = reinterpret_cast<uint16_t *>(smem + L.rings);
     uint16_t *inring = reinterpret_cast<uint16_t *>(smem + L.inring);
@@ -289,13 +308,13 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     auto bj0 = [&](int b) { return pass ? max(0, W - FB * (b + 1)) : FB * b; };
     auto bn = [&](int b) { return min(FB, W - FB * b); };
     // Hand-off batches of the records of the band above start small so that a band can begin two pixels
-    // after the band above: pixels [0,2) [2,4) then doubling up to FB, then FB at a time (FB = 8: starts
+    // after the band above: pixels [0,2) [2,4) then doubling up to HB, then HB at a time (HB = 8: starts
     // 0 2 4 8 16 24 ...). Each batch costs the writer a release and the fetcher a poll and a copy, so the
     // batches are no smaller than the row's pixel period allows. No batch wraps around the ring.
-    constexpr int NPF = (FB == 8) ? 3 : 2; // batches before the first full one
-    auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : FB * (b - NPF + 1); };
+    constexpr int NPF = HB == 8 ? 3 : (HB == 4 ? 2 : 1); // batches before the first full one (log2 HB)
+    auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : HB * (b - NPF + 1); };
     auto hend = [&](int b) { return min(W, hstart(b + 1)); };
-    auto hbatch = [&](int x) { return x < FB ? (x < 2 ? 0 : 31 - __clz(x)) : x / FB + NPF - 1; };
+    auto hbatch = [&](int x) { return x < HB ? (x < 2 ? 0 : 31 - __clz(x)) : x / HB + NPF - 1; };
 
     bool first_band = true;
     for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -328,6 +347,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
         if (threadIdx.x == 0) {
             if (!first_band)
                 for (int k = 0; k < L.nbar; k++) mbar_inval(bars + 8u * k);
+            st_release_cta_shared(relcnt, 0u);
             // ring slots: producer = the row's warp, consumer = the next row's warp or, for the last row, the
             // writer (32 arrivals each)
             for (int k = 0; k < L.nslot; k++) {
@@ -336,7 +356,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             }
             for (int wr = 0; wr < R; wr++)
                 for (int g = 0; g < 2; g++) mbar_init(cfull(wr, g), 1); // row warp's arrive.expect_tx + bytes
-            for (int b = 0; b < 2; b++) mbar_init(infull(b), 1);    // fetcher's arrive.expect_tx + bytes
+            for (int b = 0; b < NIB; b++) mbar_init(infull(b), 1);  // fetcher's arrive.expect_tx + bytes
             for (int x = 0; x < KI; x++) mbar_init(inempty(x), 32); // the first row's warp
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -379,7 +399,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             auto wait_above = [&](int x) {
                 if (from_in) {
                     const int hb = hbatch(x);
-                    if (x < W && (x == hstart(hb) || x == 1)) mbar_wait(infull(hb), (hb / 2) & 1, a);
+                    if (x < W && (x == hstart(hb) || x == 1)) mbar_wait(infull(hb), (hb / NIB) & 1, a);
                 } else {
                     mbar_wait(abar + 16u * (uint32_t)(x & (kKP - 1)), (uint32_t)(x >> 2) & 1u, a);
                 }
@@ -529,10 +549,10 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                 unsigned seen = 0;
                 for (int b = 0; b < nhb; b++) {
                     const int hs = hstart(b), he = hend(b), nb = he - hs;
-                    // before reusing barrier b & 1 the reader must be past batch b-2, and the ring slots of
+                    // before reusing barrier b % NIB the reader must be past batch b-NIB, and the ring slots of
                     // pixels hs..he-1 must be free (they last held pixels hs-KI..he-1-KI); the reader releases
                     // in pixel order, so waiting for the later of the two last pixels covers both
-                    const int y = max(b >= 2 ? hend(b - 2) - 1 : -1, he - 1 - KI);
+                    const int y = max(b >= NIB ? hend(b - NIB) - 1 : -1, he - 1 - KI);
                     if (y >= 0) mbar_wait(inempty(y), (y / KI) & 1, a);
                     const unsigned need = (unsigned)he;
                     if (seen < need) {
@@ -556,11 +576,13 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                     mbar_expect_tx(infull(b), bytes);
                     bulk_g2s(sptr(inring + (size_t)(hs % KI) * rec), src + (size_t)hs * rec, bytes, infull(b));
                 }
-                for (int b = max(0, nhb - 2); b < nhb; b++) mbar_drain(infull(b), (b / 2) & 1, a.wait_limit_us);
+                for (int b = max(0, nhb - NIB); b < nhb; b++) mbar_drain(infull(b), (b / NIB) & 1, a.wait_limit_us);
             }
         } else if (wi == R + 1 && publish) {
-            // ===================================================== writer: band's last row -> global, progress
-            // record x is complete once the last row has arrived on the slot of x+1 (x = W-1: virtual pixel W)
+            // ===================================================== writer: band's last row -> global memory
+            // record x is complete once the last row has arrived on the slot of x+1 (x = W-1: virtual pixel W).
+            // At the end of every hand-off batch the count of copied records goes to the releaser through
+            // shared memory; the writer itself never waits on a device-wide fence.
             uint16_t *dst = bnd + (size_t)band * W * rec;
             const uint16_t *lring = rings + (size_t)(R - 1) * kKP * rec;
             const uint32_t lbar = bars + 16u * (uint32_t)((R - 1) * kKP);
@@ -571,11 +593,31 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                 uint4 *g4 = reinterpret_cast<uint4 *>(dst + (size_t)x * rec);
                 for (int k = lane; k < nch; k += 32) g4[k] = s4[k];
                 mbar_arrive(lbar + 16u * (uint32_t)(x & (kKS - 1)) + 8u);
-                // releases at the end of every hand-off batch (the fetcher copies whole batches)
                 if (x + 1 == hend(hbatch(x))) {
-                    __threadfence();
+                    // the other lanes' stores are ordered before lane 0's release through the warp barrier
                     __syncwarp();
-                    if (lane == 0) st_release(progress + (size_t)band * kProgressStride, (unsigned)(x + 1));
+                    if (lane == 0) st_release_cta_shared(relcnt, (unsigned)(x + 1));
+                }
+            }
+        } else if (wi == R + 2 && publish && lane == 0) {
+            // ===================================================== releaser: copied records -> progress counter
+            // A device-scope release of the latest count (cumulative: it covers the writer's stores, which this
+            // thread acquired through the shared counter); batches that completed while a release was in flight
+            // are published together by the next one.
+            unsigned last = 0;
+            const unsigned long long t0 = global_ns();
+            for (unsigned n = 0; last < (unsigned)W; n++) {
+                const unsigned v = ld_acquire_cta_shared(relcnt);
+                if (v > last) {
+                    st_release(progress + (size_t)band * kProgressStride, v);
+                    last = v;
+                    continue;
+                }
+                __nanosleep(64);
+                if (n % kCheckEvery == kCheckEvery - 1 &&
+                    (ld_relaxed(a.err) != kErrNone || global_ns() - t0 > 1000ull * a.wait_limit_us)) {
+                    atomicCAS(a.err, kErrNone, kErrTimeout);
+                    break;
                 }
             }
         }
@@ -695,11 +737,13 @@ int sgm_rows_gb300(int dp) {
 namespace {
 // Rows per band. The plan simulates the persistent schedule: work item k (band k >> 1 of pass k & 1) runs on
 // CTA k mod (resident CTAs) after that CTA's previous item, and no earlier than one band lag after the
-// previous band of its pass; an item takes W pixel periods. A row warp's pixel period grows with the rows
-// its SM carries (issue slots are shared) above a latency floor, and the band lag is about one period per
-// row plus the hand-off (a batch of records and its release, poll and copy), so in units of one row's issue
-// time: period T = 20 + rows per SM, band lag = (1.2 R + 11) T. The band height with the earliest simulated
-// finish wins; ties go to the taller band (fewer hand-offs). per_sm(R): CTAs of band height R per SM.
+// previous band of its pass; an item takes W pixel periods. A row warp's pixel period grows with the row
+// warps that share its scheduler (four schedulers per SM; warp w runs on scheduler w mod 4, so the busiest one
+// carries ceil(rows per SM / 4)) above a latency floor, and the band lag is about 1.33 periods per row plus the
+// hand-off (a 2-pixel batch of records, its release, poll and copy: about 7 periods), so in units of one row's
+// issue time: period T = 20 + 4 ceil(rows per SM / 4), band lag = (1.33 R + 7) T. The band height with the
+// earliest simulated finish wins; ties go to the taller band (fewer hand-offs). per_sm(R): CTAs of band height
+// R per SM.
 template <class F>
 SgmPlan plan_rows(const Geom &g, int sms, int lo, int hi, F per_sm) {
     SgmPlan p{};
@@ -711,8 +755,9 @@ SgmPlan plan_rows(const Geom &g, int sms, int lo, int hi, F per_sm) {
         const int nb = (g.Hp + R - 1) / R;
         const int items = 2 * nb;
         const int conc = std::min(items, k * sms);
-        const double T = 20.0 + R * ((conc + sms - 1) / sms);
-        const double lag = (1.2 * R + 11.0) * T, sweep = (double)g.Wp * T;
+        const int rows_sm = R * ((conc + sms - 1) / sms);
+        const double T = 20.0 + 4.0 * ((rows_sm + 3) / 4);
+        const double lag = (1.33 * R + 7.0) * T, sweep = (double)g.Wp * T;
         free.assign(conc, 0.0);
         start.assign(items, 0.0);
         double end = 0;
