@@ -62,7 +62,7 @@ __host__ __device__ constexpr int hand_px(int) { return 2; }
 __host__ __device__ constexpr int in_batches(int dp) { return 2 * batch_px(dp) / hand_px(dp); }
 
 // one pixel's record, in ring slots and in the global hand-off rows alike: r1 | r2 | r3 (dp u16 each) |
-// minima m1 m2 m3 (+5 pad)
+// minima m1 m2 m3, each as a u32 pair (m, m) so that it feeds the packed arithmetic directly (+2 pad)
 __host__ __device__ inline int rec_u16(int dp) { return 3 * dp + 8; }
 
 struct SgmSmem {
@@ -237,9 +237,27 @@ __device__ __forceinline__ void stw(uint16_t *p, const uint32_t (&v)[NP]) {
     }
 }
 
+// NP consecutive 32-bit words to global memory with the streaming hint (written once, read by a later kernel)
+template <int NP>
+__device__ __forceinline__ void stg_stream(uint16_t *p, const uint32_t (&v)[NP]) {
+    if constexpr (NP % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < NP / 4; k++)
+            __stcs(reinterpret_cast<uint4 *>(p) + k, make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+    } else if constexpr (NP % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < NP / 2; k++) __stcs(reinterpret_cast<uint2 *>(p) + k, make_uint2(v[2 * k], v[2 * k + 1]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < NP; k++) __stcs(reinterpret_cast<unsigned *>(p) + k, v[k]);
+    }
+}
+
 // ---------------------------------------------------------------- packed path update
 __device__ __forceinline__ uint32_t perm_hi_lo(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
 __device__ __forceinline__ uint32_t hmin(uint32_t v) { return min(v & 0xFFFFu, v >> 16); }
+// the smaller half of v in both halves: a warp minimum of such pairs is again a pair (m, m)
+__device__ __forceinline__ uint32_t hmin2(uint32_t v) { return __vminu2(v, __byte_perm(v, 0, 0x1032)); }
 
 // remaining-lines update of one path (sgm.cpp:278-383) for this lane's DPL = 2*NP disparities:
 //   L(d) = C(d) + min(Lp(d), Lp(d-1)+7, Lp(d+1)+7, minLp+100) - minLp; returns the lane's minimum
@@ -254,8 +272,8 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
     uint32_t right = __shfl_down_sync(FULL, P[0], 1);
     if (lane == 0) left = INF2;
     if (lane == 31) right = INF2;
-    const uint32_t m2 = minLp * 0x00010001u;
-    const uint32_t p2 = (minLp + 100u) * 0x00010001u;
+    const uint32_t m2 = minLp; // (minLp, minLp)
+    const uint32_t p2 = minLp + 0x00640064u;
     uint32_t xprev = perm_hi_lo(left, P[0]); // (Lp[d-1], Lp[d]) of the first pair
     uint32_t mn = 0xFFFFFFFFu;
 #pragma unroll
@@ -270,7 +288,7 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
             mn = __vminu2(mn, v);
         xprev = x;
     }
-    return hmin(mn);
+    return hmin2(mn);
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -448,10 +466,10 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                         n3[k] = c[k] & ~__vcmpeq2(c[k], 0x00FF00FFu);
                         cmin = __vminu2(cmin, n3[k]);
                     }
-                    m3 = __reduce_min_sync(FULL, hmin(cmin));
+                    m3 = __reduce_min_sync(FULL, hmin2(cmin));
                     if (has_cons) {
                         stw<NP>(dst + 2 * dp + d0, n3);
-                        if (lane == 0) dst[3 * dp + 2] = (uint16_t)m3;
+                        if (lane == 0) *reinterpret_cast<uint32_t *>(dst + 3 * dp + 4) = m3;
                         mbar_arrive(ofull);
                     }
                     uint32_t mnv = 0xFFFFFFFFu;
@@ -473,7 +491,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                         r0[k] = g[k];
                         n1[k] = n2[k] = n3[k];
                     }
-                    r0min = __reduce_min_sync(FULL, hmin(mnv));
+                    r0min = __reduce_min_sync(FULL, hmin2(mnv));
                     m1 = m2 = m3;
                 } else {
                     // r3 reads column q+1, r2 column q, r1 column q-1 of the row above (outside the image:
@@ -484,7 +502,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                     if (q + 1 < W) {
                         const uint16_t *s3 = aring + (size_t)((q + 1) & amask) * rec;
                         ldw<NP>(s3 + 2 * dp + d0, a3);
-                        am3 = s3[3 * dp + 2];
+                        am3 = *reinterpret_cast<const uint32_t *>(s3 + 3 * dp + 4);
                     } else {
 #pragma unroll
                         for (int k = 0; k < NP; k++) a3[k] = INF2;
@@ -495,16 +513,16 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                         const uint16_t *s2 = aring + (size_t)(q & amask) * rec;
                         ldw<NP>(s2 + d0, b1);
                         ldw<NP>(s2 + dp + d0, a2);
-                        const uint32_t mm = *reinterpret_cast<const uint32_t *>(s2 + 3 * dp);
-                        bm1 = mm & 0xFFFFu;
-                        am2 = mm >> 16;
+                        const uint2 mm = *reinterpret_cast<const uint2 *>(s2 + 3 * dp);
+                        bm1 = mm.x;
+                        am2 = mm.y;
                         release_above(q);
                     }
                     // r3 first: the row below waits for it
                     m3 = __reduce_min_sync(FULL, path_step<NP>(a3, am3, c, n3, lane));
                     if (has_cons) {
                         stw<NP>(dst + 2 * dp + d0, n3);
-                        if (lane == 0) dst[3 * dp + 2] = (uint16_t)m3;
+                        if (lane == 0) *reinterpret_cast<uint32_t *>(dst + 3 * dp + 4) = m3;
                         mbar_arrive(ofull);
                     }
                     uint32_t n0[NP];
@@ -524,15 +542,17 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                 }
                 // the pass's sum: first line r0 alone (sgm.cpp:132, :187), else r0+r1+r2+r3 (:386-391); u16
                 // arithmetic never saturates or wraps for real disparities
-                stw<NP>(sp, g);
+                stg_stream<NP>(sp, g);
                 sp += sstep;
                 if (has_cons) {
                     stw<NP>(dst + d0, n1);
                     stw<NP>(dst + dp + d0, n2);
-                    if (lane == 0) *reinterpret_cast<uint32_t *>(dst + 3 * dp) = m1 | (m2 << 16);
-                    // the slot of pixel q+1 last held pixel q+1-ns (waited for here, off the r3 path)
-                    const int y = q + 1 - ns;
-                    if (y >= 0) mbar_wait(obar + 16u * (uint32_t)((q + 1) & (ns - 1)) + 8u, (uint32_t)(y >> lgs) & 1u, a);
+                    if (lane == 0) *reinterpret_cast<uint2 *>(dst + 3 * dp) = make_uint2(m1, m2);
+                    // the slots of pixels q+1 and q+2 last held pixels q+1-ns and q+2-ns; at even q one wait for the
+                    // later release covers both (the row below releases in pixel order)
+                    const int y = q + 2 - ns;
+                    if (!(q & 1) && y >= 0)
+                        mbar_wait(obar + 16u * (uint32_t)((q + 2) & (ns - 1)) + 8u, (uint32_t)(y >> lgs) & 1u, a);
                 }
             }
             // virtual pixel W: publishes r1 and r2 of the last pixel
