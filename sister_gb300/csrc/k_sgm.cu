@@ -735,6 +735,7 @@ void init_sgm_kernels() {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     for (int dpl : kDplChoices) cudaFuncSetAttribute(kernel_for(dpl), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaGetLastError();
+    init_cost_kernels();
 }
 
 // largest band height whose shared-memory layout fits this device

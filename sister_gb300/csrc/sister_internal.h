@@ -67,6 +67,7 @@ struct SgmPlan {
 // one-time per-device kernel attribute setup (dynamic shared memory limits)
 void init_mask_kernels();
 void init_sgm_kernels();
+void init_cost_kernels(); // shared-memory limit of the cost kernels on this device
 
 // ---- kernel launchers (all asynchronous on `st`) ----
 // views_dev: 5 planes of w*h gray bytes, tightly packed, order {center, right, top, left, bottom}
