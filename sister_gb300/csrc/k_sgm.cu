@@ -440,6 +440,9 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             const ptrdiff_t sstep = pass ? -(ptrdiff_t)dp : (ptrdiff_t)dp;
             const uint16_t *cg = myc;
             int cn = 0;
+            // unrolled by two: the second pixel takes its predecessor's states without register copies
+            // (4.08 against 4.25 ms on 1920x1080/256; by four the loop outgrows the instruction cache, 4.40 ms)
+#pragma unroll 2
             for (int q = 0; q < W; q++) {
                 const int t = q % FB;
                 if (t == 0) {
