@@ -43,9 +43,9 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # aggregation (both passes), final WTA
 KERNELS_PER_COMPUTE = 7
 # DRAM bytes per padded cell of one aggregation launch, measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.822 + 1.080 GB for 992*832*256 cells. It exceeds
+# dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.817 + 1.110 GB for 992*832*256 cells. It exceeds
 # the 8 algorithmic bytes per cell by the band hand-off records; scaled to other rigs by the cell count.
-TRAFFIC_BYTES_PER_CELL = (0.822244352e9 + 1.080090e9) / (992 * 832 * 256)
+TRAFFIC_BYTES_PER_CELL = (0.816880640e9 + 1.109881e9) / (992 * 832 * 256)
 
 
 def rig_units() -> float:
@@ -392,7 +392,7 @@ def run_gb300(args):
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": TRAFFIC_BYTES_PER_CELL * cells,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of sgm_kernel<8> on a 480x320/256 "
-                                  "rig (1.90 GB for 211 M padded cells), scaled to this launch by the cell count",
+                                  "rig (1.93 GB for 211 M padded cells), scaled to this launch by the cell count",
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": 8 * cells, "launch_ms": avg}
 
     if rank == 0:
