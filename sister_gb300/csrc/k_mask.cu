@@ -43,7 +43,7 @@ __device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b
     const int b = b0 + lane;
     // OR masks: a shuffled cell i counts for this lane's row when i <= lane, else for the entering row
     const uint32_t m1 = lane >= 1 ? 0u : ~0u, m2 = lane >= 2 ? 0u : ~0u, m3 = lane >= 3 ? 0u : ~0u;
-#pragma unroll 2
+#pragma unroll 8 // 8.74 against 8.90 ms per 1920x1080/256 rig for 2
     for (int d = 0; d < dmax; d += 4) {
         const int a = b + d;
         uint32_t k[4];
