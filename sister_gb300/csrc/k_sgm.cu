@@ -325,10 +325,10 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     // are contiguous, ascending in pass 0 and descending in pass 1. first column (lowest j) and pixel count:
     auto bj0 = [&](int b) { return pass ? max(0, W - FB * (b + 1)) : FB * b; };
     auto bn = [&](int b) { return min(FB, W - FB * b); };
-    // Hand-off batches of the records of the band above start small so that a band can begin two pixels
-    // after the band above: pixels [0,2) [2,4) then doubling up to HB, then HB at a time (HB = 8: starts
-    // 0 2 4 8 16 24 ...). Each batch costs the writer a release and the fetcher a poll and a copy, so the
-    // batches are no smaller than the row's pixel period allows. No batch wraps around the ring.
+    // Hand-off batches of the records of the band above: pixels [0,2) [2,4) then doubling up to HB, then HB at a
+    // time (HB = 2: starts 0 2 4 6 ...; HB = 8: 0 2 4 8 16 24 ...), so a band can begin two pixels after the band
+    // above. Each batch costs the writer a shared-memory count, the releaser a device-scope release and the
+    // fetcher a poll and a copy. No batch wraps around the ring.
     constexpr int NPF = HB == 8 ? 3 : (HB == 4 ? 2 : 1); // batches before the first full one (log2 HB)
     auto hstart = [&](int b) { return b < NPF ? (b == 0 ? 0 : (1 << b)) : HB * (b - NPF + 1); };
     auto hend = [&](int b) { return min(W, hstart(b + 1)); };
