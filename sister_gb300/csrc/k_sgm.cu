@@ -20,8 +20,8 @@
 //     the next two pixels. The four updates are independent, so they overlap; the warp adds them into the
 //     pass's sum itself. A row therefore trails the row above by about one pixel;
 //   * every row hands its new r1|r2|r3 states and their minima (one record per pixel) to the row below
-//     through a ring of kKP slots with a full and an empty barrier per slot; producers check the empty
-//     barriers once per half ring;
+//     through a ring of kKP slots with a full and an empty barrier per slot; producers wait on the empty
+//     barriers once per two pixels;
 //   * data from global memory arrives by bulk copies (TMA). A warp completes about one asynchronous copy
 //     per global-memory round trip however large it is (measured on GB300: ~500-750 cycles per copy for
 //     anything from 512 B to 16 KB), so every stream is copied in batches: the cost rows of FB
@@ -674,15 +674,25 @@ __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict
     uint32_t s0[NP], s1[NP];
     ldw<NP>(s0v + pix * g.dp + d0, s0);
     ldw<NP>(s1v + pix * g.dp + d0, s1);
-    // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums are smaller)
+    // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums are smaller). Pixels
+    // with j >= dp-1 in a volume whose stride holds only real disparities (dc = dp) need neither test (warp-uniform)
     uint32_t best = 0xFFFFFFFFu;
+    if (j >= g.dp - 1 && D == g.dp) {
 #pragma unroll
-    for (int k = 0; k < NP; k++) {
-        const int d = d0 + 2 * k;
-        uint32_t sv = s0[k] + s1[k]; // both halves of a pair are real or both infinite (dc % 8 == 0)
-        if (d >= D || d > j) sv |= 0x0000FFFFu;
-        if (d + 1 >= D || d + 1 > j) sv |= 0xFFFF0000u;
-        best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+        for (int k = 0; k < NP; k++) {
+            const int d = d0 + 2 * k;
+            const uint32_t sv = s0[k] + s1[k];
+            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const int d = d0 + 2 * k;
+            uint32_t sv = s0[k] + s1[k]; // both halves of a pair are real or both infinite (dc % 8 == 0)
+            if (d >= D || d > j) sv |= 0x0000FFFFu;
+            if (d + 1 >= D || d + 1 > j) sv |= 0xFFFF0000u;
+            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+        }
     }
     best = __reduce_min_sync(FULL, best);
     if (lane == 0) {
