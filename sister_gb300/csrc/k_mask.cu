@@ -332,28 +332,40 @@ __global__ void __launch_bounds__(1024) wta_median_kernel(const uint64_t *__rest
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) and the mask loops of SisterMultiviewDisparities.hpp:201-251:
 // keep = L <= j && |L - R[j-L]| <= 5; mask = keep && L > 0 && j >= dc; written in padded original
 // coordinates (frame 2: (i, Wp-1-j); frame 1: transpose + flip(-1); frame 3: transpose + flip(1)).
+// 32x32 tiles of frame coordinates (a, b); the transposed frames 1 and 3 go through a shared tile so that their
+// mask rows (padded image rows i = Hp-1-b or b, columns j = Wp-1-a) are written contiguously too.
 __global__ void lrc_mask_kernel(const uint16_t *__restrict__ med, Geom g, uint8_t *__restrict__ masks, int f0) {
+    __shared__ uint8_t tile[32][33];
     const int f = f0 + blockIdx.z;
     const int H = g.frows(f), W = g.fcols(f);
-    const int b = blockIdx.x * blockDim.x + threadIdx.x, a = blockIdx.y;
-    if (a >= H || b >= W) return;
-    const uint16_t *L = med + (size_t)(2 * f) * g.plane + (size_t)a * W;
-    const uint16_t *R = med + (size_t)(2 * f + 1) * g.plane + (size_t)a * W;
-    const int base = L[b];
-    bool keep = false;
-    if (base <= b) {
-        const int diff = base - (int)R[b - base];
-        keep = diff <= 5 && diff >= -5;
+    const int a0 = blockIdx.y * 32, b0 = blockIdx.x * 32;
+    if (a0 >= H || b0 >= W) return; // block-uniform
+    const int tx = threadIdx.x, ty = threadIdx.y; // 32 x 8
+    uint8_t *out = masks + (size_t)f * g.plane;
+    for (int s = ty; s < 32; s += 8) {
+        const int a = a0 + s, b = b0 + tx;
+        uint8_t m = 0;
+        if (a < H && b < W) {
+            const uint16_t *L = med + (size_t)(2 * f) * g.plane + (size_t)a * W;
+            const uint16_t *R = med + (size_t)(2 * f + 1) * g.plane + (size_t)a * W;
+            const int base = L[b];
+            bool keep = false;
+            if (base <= b) {
+                const int diff = base - (int)R[b - base];
+                keep = diff <= 5 && diff >= -5;
+            }
+            m = (keep && base > 0 && b >= g.dc) ? 1 : 0;
+            if (!(f & 1)) out[(size_t)a * g.Wp + (f == 0 ? b : g.Wp - 1 - b)] = m;
+        }
+        tile[s][tx] = m;
     }
-    const uint8_t m = (keep && base > 0 && b >= g.dc) ? 1 : 0;
-    int i, j;
-    switch (f) {
-    case 0: i = a; j = b; break;
-    case 2: i = a; j = g.Wp - 1 - b; break;
-    case 1: i = g.Hp - 1 - b; j = g.Wp - 1 - a; break;
-    default: i = b; j = g.Wp - 1 - a; break;
+    if (f & 1) {
+        __syncthreads();
+        for (int s = ty; s < 32; s += 8) {
+            const int b = b0 + s, a = a0 + tx; // consecutive a: consecutive (descending) columns j = Wp-1-a
+            if (a < H && b < W) out[(size_t)(f == 1 ? g.Hp - 1 - b : b) * g.Wp + (g.Wp - 1 - a)] = tile[tx][s];
+        }
     }
-    masks[(size_t)f * g.plane + (size_t)i * g.Wp + j] = m;
 }
 
 // doLRCheck(L, R, W, H, 5) (postprocess.cpp:318-341) as the two-view doStereo applies it (hpp:145): the left map
@@ -425,7 +437,7 @@ void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16
 
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0, int nf) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    lrc_mask_kernel<<<dim3((mx + 255) / 256, mx, nf), 256, 0, st>>>(med, g, masks, f0);
+    lrc_mask_kernel<<<dim3((mx + 31) / 32, (mx + 31) / 32, nf), dim3(32, 8), 0, st>>>(med, g, masks, f0);
 }
 
 } // namespace sister
