@@ -133,8 +133,13 @@ enum {
     SISTER_TUNE_SGM_CLUSTER = 2,  /* CTAs per thread-block cluster (1, 2, 4 or 8); 0 = automatic */
     SISTER_TUNE_SGM_GROUPS = 3,   /* read-only: cluster-sized row groups of the current geometry */
     SISTER_TUNE_SGM_CLUSTERS = 4, /* read-only: co-resident clusters launched */
-    SISTER_TUNE_FULL_DISP = 5     /* 1: also write the padded winner-take-all map (SISTER_DBG_DISP); 0 (default):
+    SISTER_TUNE_FULL_DISP = 5,    /* 1: also write the padded winner-take-all map (SISTER_DBG_DISP); 0 (default):
                                      only the cropped outputs are computed */
+    SISTER_TUNE_WAIT_LIMIT_US = 6 /* longest device-side wait of one warp on another warp or CTA (band hand-offs,
+                                     median row flags) before the kernel gives up, raises its error flag and
+                                     finishes: the compute then returns SISTER_ETIMEOUT and the context stays
+                                     usable. 0 = default (2 s). A small value makes waits expire on purpose
+                                     (tests of the failure path). */
 };
 /* Set a knob for subsequent computes (no reference counterpart: the reference is single-threaded CPU code). */
 SISTER_API int sister_tune_set(sister_ctx *ctx, int key, int value);

@@ -111,3 +111,8 @@ class MultiviewDisparities {
 };
 
 } // namespace sister
+
+// The reference's class name at global scope (SisterMultiviewDisparities.hpp:18), so callers written against the
+// reference -- compute_disp.cpp:26-35 constructs `SisterMultiviewDisparities multiview(center, right, top, left,
+// bottom)` -- compile unchanged once this header replaces the reference's include.
+using SisterMultiviewDisparities = sister::MultiviewDisparities;

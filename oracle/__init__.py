@@ -35,18 +35,32 @@ def build_port(force: bool = False) -> str:
     return PORT_SO
 
 
-def reference_available() -> bool:
-    return os.path.isdir(os.environ.get("SISTER_REFERENCE", "/root/reference") + "/cpp/src/sister") and \
-        platform.machine().lower() in ("x86_64", "amd64")
-
-
-def build_ref(force: bool = False) -> str | None:
-    """Compile the reference's stage sources + glue; None when the reference cannot be built here."""
-    if not reference_available():
+def reference_tree() -> str | None:
+    """The reference project tree named by SISTER_REFERENCE, when it is present and this host can compile its
+    SSE4.1 stage code (x86-64); None otherwise."""
+    ref = os.environ.get("SISTER_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "cpp", "src", "sister")):
         return None
-    if force or not os.path.exists(REF_SO):
-        subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")], stdout=subprocess.DEVNULL)
-    return REF_SO
+    return ref if platform.machine().lower() in ("x86_64", "amd64") else None
+
+
+def reference_available() -> bool:
+    """The reference's compiled stage code can be loaded: already built into oracle/_ref (on an x86-64 host), or
+    buildable from the tree named by SISTER_REFERENCE."""
+    if platform.machine().lower() not in ("x86_64", "amd64"):
+        return False
+    return os.path.exists(REF_SO) or reference_tree() is not None
+
+
+def build_ref(force: bool = False, tree: str | None = None) -> str | None:
+    """Compile the reference's stage sources + glue from `tree` (default: SISTER_REFERENCE) into oracle/_ref;
+    returns the library path, or None when it cannot be built or loaded here."""
+    if tree:
+        os.environ["SISTER_REFERENCE"] = tree
+    src = reference_tree()
+    if src and (force or not os.path.exists(REF_SO)):
+        subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), src], stdout=subprocess.DEVNULL)
+    return REF_SO if reference_available() and os.path.exists(REF_SO) else None
 
 
 def _ptr(a: np.ndarray, t):
@@ -66,6 +80,7 @@ class Port(_Lib):
         super().__init__(path or build_port())
         L = self.lib
         L.orc_compute.restype = ctypes.c_int
+        L.orc_compute_stream.restype = ctypes.c_int
         L.orc_num_threads.restype = ctypes.c_int
 
     @staticmethod
@@ -186,6 +201,19 @@ class Port(_Lib):
         if rc != 0:
             raise RuntimeError("orc_compute failed with %d" % rc)
         return (*outs, mk) if masks else tuple(outs)
+
+    def compute_stream(self, views, dc, mode: int = 0, padded: bool = False):
+        """One mode of compute_disparities in bounded memory (orc_compute_stream): returns the w x h output,
+        or (output, padded disparity map) with padded=True."""
+        h, w = views[0].shape
+        vs, arr = self._views(views)
+        out = np.zeros((h, w), np.uint16)
+        pad = np.zeros((h + 2 * dc, w + 2 * dc), np.uint16) if padded else None
+        rc = self.lib.orc_compute_stream(arr, w, h, dc, int(mode), _ptr(out, _u16p),
+                                         _ptr(pad, _u16p) if pad is not None else None)
+        if rc != 0:
+            raise RuntimeError("orc_compute_stream failed with %d" % rc)
+        return (out, pad) if padded else out
 
 
 class Ref(_Lib):

@@ -1,9 +1,11 @@
 #!/usr/bin/env bash
 # TEST INFRASTRUCTURE: compile the reference's own stage sources, unmodified and in place, together with
 # oracle/ref_glue.cpp into oracle/_ref/libsister_ref.so. The reference needs SSE4.1/4.2 intrinsics, so
-# this only builds on x86-64 hosts that have the reference tree (default /root/reference).
+# this only builds on x86-64 hosts that have the reference tree, named by the first argument or SISTER_REFERENCE.
+#     bash oracle/build_ref.sh REFERENCE_TREE
 set -euo pipefail
-REF="${SISTER_REFERENCE:-/root/reference}"
+REF="${1:-${SISTER_REFERENCE:-}}"
+if [ -z "$REF" ]; then echo "usage: build_ref.sh REFERENCE_TREE (or set SISTER_REFERENCE)" >&2; exit 2; fi
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/cpp/src/sister" ]; then echo "reference tree not found at $REF" >&2; exit 3; fi

@@ -462,6 +462,239 @@ void orc_crop_scale(const uint16_t *disp, int Wp, int dc, int w, int h, uint16_t
         }
 }
 
+/* Pre-aggregation stages of compute_disparities (hpp:29-70, :188-252): frames, census and the four confidence
+ * masks in padded original coordinates. census: 8 * Wp*Hp words, masks: 4 * Wp*Hp bytes. Returns 0, or 2 when
+ * memory runs out. */
+static int prep_stages(const uint8_t *const views[5], int w, int h, int dc, uint64_t *census, uint8_t *masks) {
+    const int Wp = w + 2 * dc, Hp = h + 2 * dc;
+    const size_t plane = (size_t)Wp * Hp;
+    uint8_t *frames = (uint8_t *)malloc(8 * plane);
+    uint8_t *mframe = (uint8_t *)malloc(plane);
+    uint16_t *L = (uint16_t *)malloc(plane * 2), *R = (uint16_t *)malloc(plane * 2);
+    int rc = 2;
+    if (frames && mframe && L && R) {
+        orc_frames(views, w, h, dc, frames);
+        for (int k = 0; k < 8; k++) {
+            const int f = k / 2, rows = (f & 1) ? Wp : Hp, cols = (f & 1) ? Hp : Wp;
+            orc_census(frames + k * plane, cols, rows, census + k * plane);
+        }
+        for (int f = 0; f < 4; f++) {
+            const int rows = (f & 1) ? Wp : Hp, cols = (f & 1) ? Hp : Wp;
+            orc_wta_lr(census + (2 * f) * plane, census + (2 * f + 1) * plane, cols, rows, dc, L, R);
+            orc_median_inplace(L, cols, rows);
+            orc_median_inplace(R, cols, rows);
+            orc_lrc_mask(L, R, cols, rows, dc, mframe);
+            orc_mask_to_orig(mframe, f, Wp, Hp, masks + f * plane);
+        }
+        rc = 0;
+    }
+    free(frames); free(mframe); free(L); free(R);
+    return rc;
+}
+
+/* One row i of the masked multiview cost (the loop body of hpp:255-277 for a fixed i): Wp * D cells. */
+static void masked_cost_row(const uint64_t *const census[8], const uint8_t *const masks[4], int Wp, int Hp, int D,
+                            int mode, int i, uint16_t *row) {
+    const int use[4] = {mode != 2, mode != 1, mode != 2, mode != 1};
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < Wp; j++) {
+        const size_t p = (size_t)i * Wp + j;
+        int m[4];
+        for (int f = 0; f < 4; f++) m[f] = use[f] ? masks[f][p] : 0;
+        uint16_t *out = row + (size_t)j * D;
+        for (int d = 0; d < D; d++) {
+            uint32_t s = 0;
+            for (int f = 0; f < 4; f++)
+                if (m[f]) s += frame_cost(census, f, Wp, Hp, i, j, d);
+            out[d] = (uint16_t)s;
+        }
+    }
+}
+
+/* One remaining-lines path update of sgm.cpp:278-383 for one pixel: L(d) = C(d) +s (min(Lp(d), Lp(d-1) +s 7,
+ * Lp(d+1) +s 7, minLp +s 100) -s minLp), Lp with guard slots Lp[-1] = Lp[D] = 65535; returns min L. */
+static inline uint16_t path_update(const uint16_t *c, const uint16_t *lp, uint16_t mlp, uint16_t *ln, int D) {
+    const uint16_t q = adds16(100, mlp);
+    uint16_t mn = INF16;
+    for (int d = 1; d <= D; d++) {
+        const uint16_t v =
+            adds16(c[d - 1], subs16(min16(min16(lp[d], min16(adds16(lp[d - 1], 7), adds16(lp[d + 1], 7))), q), mlp));
+        ln[d] = v;
+        if (v < mn) mn = v;
+    }
+    return mn;
+}
+
+/* compute_disparities for one mode, restated in bounded memory for rigs whose volumes do not fit twice in host
+ * memory (4096x3000 at dc 512: 21.1 GB per u16 volume). Same arithmetic as orc_compute, organised differently:
+ *  - the masked cost M (hpp:255-277) is never stored: each pass recomputes row i of M from the census words and
+ *    masks when it reaches that row;
+ *  - the pass-0 sum is the only volume held (Hp*Wp*dc u16); pass 1 adds to it row by row (sgm.cpp:187, :390)
+ *    and, once a row is final, takes its WTALeft (hpp:283) into the padded map at once;
+ *  - within a row, path r0 (sgm.cpp:215-297, restarted per row) runs first along the row; r1, r2 and r3 read
+ *    only the previous row's states (double-buffered here instead of updated in place), so their pixels are
+ *    independent and run in parallel; the per-pixel sum keeps the reference's order ((r0 + r1) + r2) + r3 with
+ *    u16 saturation (sgm.cpp:388).
+ * The first line of each pass follows sgm.cpp:103-207 exactly as orc_sgm_passes does. out: w*h (crop, *255),
+ * disp_padded: Hp*Wp (may be NULL). Returns 0, 1 on bad arguments, 2 when memory runs out. */
+int orc_compute_stream(const uint8_t *const views[5], int w, int h, int dc, int mode, uint16_t *out,
+                       uint16_t *disp_padded) {
+    if (w < 4 || h < 4 || dc < 8 || dc % 8 || w % 4 || h % 4 || mode < 0 || mode > 2 || !out) return 1;
+    for (int k = 0; k < 5; k++)
+        if (!views[k]) return 1;
+    const int Wp = w + 2 * dc, Hp = h + 2 * dc, D = dc, P = D + 2, W = Wp, H = Hp;
+    const size_t plane = (size_t)Wp * Hp;
+    const size_t colsz = (size_t)(W + 2) * P;
+    int rc = 2;
+    uint64_t *census = (uint64_t *)malloc(8 * plane * sizeof(uint64_t));
+    uint8_t *masks = (uint8_t *)calloc(4 * plane, 1);
+    uint16_t *disp = (uint16_t *)malloc(plane * 2);
+    uint16_t *S = (uint16_t *)malloc(plane * (size_t)D * 2);
+    uint16_t *crow = (uint16_t *)malloc((size_t)W * D * 2);
+    uint16_t *r0row = (uint16_t *)malloc((size_t)W * D * 2); /* r0 of every pixel of the row */
+    uint16_t *st[6];                                           /* r1, r2, r3 states: last and current row */
+    uint16_t *mn[6];
+    for (int k = 0; k < 6; k++) {
+        st[k] = (uint16_t *)malloc(colsz * 2);
+        mn[k] = (uint16_t *)calloc(W + 2, 2);
+    }
+    uint16_t *r0a = (uint16_t *)malloc(P * 2), *r0b = (uint16_t *)malloc(P * 2);
+    int ok = census && masks && disp && S && crow && r0row && r0a && r0b;
+    for (int k = 0; k < 6; k++) ok = ok && st[k] && mn[k];
+    if (!ok) goto done;
+    rc = prep_stages(views, w, h, dc, census, masks);
+    if (rc) goto done;
+    {
+        const uint64_t *cptr[8];
+        for (int k = 0; k < 8; k++) cptr[k] = census + k * plane;
+        const uint8_t *mptr[4] = {masks, masks + plane, masks + 2 * plane, masks + 3 * plane};
+        for (int k = 0; k < 6; k++)
+            for (size_t q = 0; q < colsz; q++) st[k][q] = INF16;
+        /* st[0..2]: r1, r2, r3 of the previous row; st[3..5]: of the row being computed */
+#define ST(arr, c, d) (arr)[(size_t)((c) + 1) * P + (d) + 1]
+        for (int pass = 0; pass < 2; pass++) {
+            const int di = pass ? -1 : 1, dj = di;
+            const int i1 = pass ? H - 1 : 0, j1 = pass ? W - 1 : 0;
+            const int iend = pass ? -1 : H, jend = pass ? -1 : W;
+            for (int k = 0; k < 6; k++) {
+                for (size_t q = 0; q < colsz; q++) st[k][q] = INF16;
+                memset(mn[k], 0, (size_t)(W + 2) * 2);
+            }
+            /* ---- first line (sgm.cpp:103-207) ---- */
+            masked_cost_row(cptr, mptr, Wp, Hp, D, mode, i1, crow);
+            {
+                uint16_t *s = S + (size_t)i1 * W * D;
+                uint16_t r0min = 0;
+                for (int k = 0; k < P; k++) r0a[k] = r0b[k] = INF16;
+                for (int j = j1; j != jend; j += dj) {
+                    const uint16_t *c = crow + (size_t)j * D;
+                    uint16_t *sj = s + (size_t)j * D;
+                    uint16_t mnc = INF16, mn0 = INF16;
+                    for (int d = 0; d < D; d++) {
+                        const uint16_t v = c[d] == 255 ? 0 : c[d];
+                        ST(st[0], j, d) = v;
+                        ST(st[1], j, d) = v;
+                        ST(st[2], j, d) = v;
+                        if (v < mnc) mnc = v;
+                        uint16_t nv;
+                        if (j == j1) {
+                            nv = v;
+                        } else {
+                            int32_t prop = r0a[d + 1];
+                            int32_t t = (int32_t)r0a[d] + 7;
+                            if (prop > t) prop = t;
+                            t = (int32_t)r0a[d + 2] + 7;
+                            if (prop > t) prop = t;
+                            t = (int32_t)r0min + 100;
+                            if (prop > t) prop = t;
+                            prop -= r0min;
+                            nv = (uint16_t)(uint8_t)((int32_t)v + prop);
+                        }
+                        r0b[d + 1] = nv;
+                        if (nv < mn0) mn0 = nv;
+                        sj[d] = pass ? (uint16_t)(sj[d] + nv) : nv;
+                    }
+                    mn[0][j + 1] = mn[1][j + 1] = mn[2][j + 1] = mnc;
+                    uint16_t *tmp = r0a; r0a = r0b; r0b = tmp;
+                    r0min = j == j1 ? mnc : mn0;
+                }
+            }
+            if (pass) {
+#pragma omp parallel for schedule(static)
+                for (int j = 0; j < W; j++) {
+                    const uint16_t *c = S + ((size_t)i1 * W + j) * D;
+                    const int end = j < D - 1 ? j : D - 1;
+                    int best = 0;
+                    for (int d = 1; d <= end; d++)
+                        if (c[d] < c[best]) best = d;
+                    disp[(size_t)i1 * W + j] = (uint16_t)best;
+                }
+            }
+            /* ---- remaining lines (sgm.cpp:213-440) ---- */
+            for (int i = i1 + di; i != iend; i += di) {
+                masked_cost_row(cptr, mptr, Wp, Hp, D, mode, i, crow);
+                /* r0 along the row: restarts from Lp = 0, minLp = 0 (sgm.cpp:215-216) */
+                {
+                    for (int k = 0; k < P; k++) r0a[k] = INF16;
+                    for (int d = 0; d < D; d++) r0a[d + 1] = 0;
+                    uint16_t r0min = 0;
+                    for (int j = j1; j != jend; j += dj) {
+                        r0b[0] = r0b[D + 1] = INF16;
+                        const uint16_t m0 = path_update(crow + (size_t)j * D, r0a, r0min, r0b, D);
+                        memcpy(r0row + (size_t)j * D, r0b + 1, (size_t)D * 2);
+                        uint16_t *tmp = r0a; r0a = r0b; r0b = tmp;
+                        r0min = m0;
+                    }
+                }
+                uint16_t *S_row = S + (size_t)i * W * D;
+#pragma omp parallel for schedule(static)
+                for (int j = 0; j < W; j++) {
+                    uint16_t n1[P], n2[P], n3[P];
+                    n1[0] = n2[0] = n3[0] = n1[D + 1] = n2[D + 1] = n3[D + 1] = INF16;
+                    const uint16_t *c = crow + (size_t)j * D;
+                    const uint16_t m1 = path_update(c, &ST(st[0], j - dj, -1), mn[0][j - dj + 1], n1, D);
+                    const uint16_t m2 = path_update(c, &ST(st[1], j, -1), mn[1][j + 1], n2, D);
+                    const uint16_t m3 = path_update(c, &ST(st[2], j + dj, -1), mn[2][j + dj + 1], n3, D);
+                    const uint16_t *v0 = r0row + (size_t)j * D;
+                    uint16_t *s = S_row + (size_t)j * D;
+                    for (int d = 0; d < D; d++) {
+                        const uint16_t ges = adds16(adds16(adds16(v0[d], n1[d + 1]), n2[d + 1]), n3[d + 1]);
+                        s[d] = pass ? adds16(s[d], ges) : ges;
+                    }
+                    memcpy(&ST(st[3], j, 0), n1 + 1, (size_t)D * 2);
+                    memcpy(&ST(st[4], j, 0), n2 + 1, (size_t)D * 2);
+                    memcpy(&ST(st[5], j, 0), n3 + 1, (size_t)D * 2);
+                    mn[3][j + 1] = m1;
+                    mn[4][j + 1] = m2;
+                    mn[5][j + 1] = m3;
+                    if (pass) { /* the row's sums are final: WTALeft (hpp:283) */
+                        const int end = j < D - 1 ? j : D - 1;
+                        int best = 0;
+                        for (int d = 1; d <= end; d++)
+                            if (s[d] < s[best]) best = d;
+                        disp[(size_t)i * W + j] = (uint16_t)best;
+                    }
+                }
+                for (int k = 0; k < 3; k++) {
+                    uint16_t *t = st[k]; st[k] = st[k + 3]; st[k + 3] = t;
+                    t = mn[k]; mn[k] = mn[k + 3]; mn[k + 3] = t;
+                }
+            }
+        }
+#undef ST
+        orc_crop_scale(disp, Wp, dc, w, h, out);
+        if (disp_padded) memcpy(disp_padded, disp, plane * 2);
+        rc = 0;
+    }
+done:
+    free(census); free(masks); free(disp); free(S); free(crow); free(r0row); free(r0a); free(r0b);
+    for (int k = 0; k < 6; k++) {
+        free(st[k]);
+        free(mn[k]);
+    }
+    return rc;
+}
+
 int orc_compute(const uint8_t *const views[5], int w, int h, int dc, uint16_t *out_multi, uint16_t *out_h,
                 uint16_t *out_v, uint8_t *masks_out) {
     if (w < 4 || h < 4 || dc < 8 || dc % 8 || w % 4 || h % 4) return 1;

@@ -75,6 +75,14 @@ void orc_crop_scale(const uint16_t *disp, int Wp, int dc, int w, int h, uint16_t
 int orc_compute(const uint8_t *const views[5], int w, int h, int dc, uint16_t *out_multi, uint16_t *out_h,
                 uint16_t *out_v, uint8_t *masks_out);
 
+/* One mode of compute_disparities in bounded host memory (the masked cost recomputed row by row, only the
+ * pass-0 sum volume stored, the final WTA taken as pass 1 completes each row): same results as orc_compute,
+ * for rigs too large to hold the cost and sum volumes together. mode 0 multiview, 1 horizontal, 2 vertical;
+ * out = w*h (disparity*255), disp_padded = Hp*Wp padded disparity or NULL. Returns 0, 1 (bad arguments) or 2
+ * (out of memory). */
+int orc_compute_stream(const uint8_t *const views[5], int w, int h, int dc, int mode, uint16_t *out,
+                       uint16_t *disp_padded);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int orc_num_threads(void);
 

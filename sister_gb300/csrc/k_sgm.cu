@@ -563,7 +563,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             // every copy this warp issued has been waited for; after a timeout a wait may have returned
             // early, so make sure none is still in flight before the barriers are reused
             if (lane == 0)
-                for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(cfull(w, b), (b / 2) & 1, a.wait_limit_us);
+                for (int b = max(0, nbat - 2); b < nbat; b++) mbar_drain(cfull(w, b), (b / 2) & 1, kDrainLimitUs);
         } else if (wi == R && band > 0) {
             // ===================================================== fetcher: records of the band above -> inring
             if (lane == 0) {
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                     mbar_expect_tx(infull(b), bytes);
                     bulk_g2s(sptr(inring + (size_t)(hs % KI) * rec), src + (size_t)hs * rec, bytes, infull(b));
                 }
-                for (int b = max(0, nhb - NIB); b < nhb; b++) mbar_drain(infull(b), (b / NIB) & 1, a.wait_limit_us);
+                for (int b = max(0, nhb - NIB); b < nhb; b++) mbar_drain(infull(b), (b / NIB) & 1, kDrainLimitUs);
             }
         } else if (wi == R + 1 && publish) {
             // ===================================================== writer: band's last row -> global memory
@@ -849,7 +849,8 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
     return (size_t)std::max(p.ngroups, 1) * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
 }
 
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st) {
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
+                       unsigned wait_limit_us) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
     const void *fn = kernel_for(g.dpl);
     if (!fn) return cudaErrorInvalidValue;
@@ -865,7 +866,7 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
     a.R = p.R;
     a.dp = g.dp;
     a.err = err;
-    a.wait_limit_us = 2000000; // 2 s
+    a.wait_limit_us = wait_limit_us;
     cudaError_t e = cudaMemsetAsync(rig.progress, 0, progress_bytes(p.ngroups), st);
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&a};
@@ -876,7 +877,7 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
 }
 
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
-                             unsigned *err, int device, cudaStream_t st) {
+                             unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us) {
     const int dpl = dp / 32;
     const void *fn = kernel_for(dpl);
     if (!fn || R < 1 || nitems < 1) return cudaErrorInvalidValue;
@@ -895,7 +896,7 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
     a.R = R;
     a.dp = dp;
     a.err = err;
-    a.wait_limit_us = 2000000; // 2 s
+    a.wait_limit_us = wait_limit_us;
     void *args[] = {(void *)&a};
     return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R + kHelpers) * 32), args,
                                        sgm_smem(R, dp).total, st);

@@ -69,6 +69,7 @@ struct sister_ctx {
     int plan_w = 0, plan_h = 0, plan_dc = 0;
     int tune_rows = 0, tune_cs = 0;
     bool full_disp = false; // keep the padded disparity map (debug inspection)
+    unsigned wait_limit_us = kDefaultWaitUs; // limit of every device-side wait on another warp or CTA
     // stage profiling: events recorded on the context stream around every stage of a compute
     bool prof = false;
     std::vector<cudaEvent_t> ev;
@@ -230,7 +231,7 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     // profiling on, the pair WTA stage covers that launch and the median stage is empty.
     if (++c->epoch == 0) c->epoch = 1;
     launch_wta_median(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), c->med.as<uint16_t>(),
-                      c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st);
+                      c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st, c->wait_limit_us);
     c->mark(SISTER_STAGE_PAIR_WTA);
     c->mark(SISTER_STAGE_MEDIAN);
     launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
@@ -248,7 +249,7 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.sum1 = c->sum1.as<uint16_t>();
         a.bnd = c->bnd.as<uint16_t>();
         a.progress = c->progress.as<unsigned>();
-        e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st);
+        e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st, c->wait_limit_us);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->mark(SISTER_STAGE_AGGREGATE);
         e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode],
@@ -429,7 +430,7 @@ int sister_stereo(sister_ctx *c, const uint8_t *center, const uint8_t *other, in
     a.sum1 = c->sum1.as<uint16_t>();
     a.bnd = c->bnd.as<uint16_t>();
     a.progress = c->progress.as<unsigned>();
-    e = launch_sgm(g, p, a, c->errflag.as<unsigned>(), st);
+    e = launch_sgm(g, p, a, c->errflag.as<unsigned>(), st, c->wait_limit_us);
     if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
     // WTALeft / WTARight (hpp:141-142) into maps 0 and 1 of frame 0, their in-place medians (hpp:143-144), LR check
     uint16_t *wta = c->wta.as<uint16_t>();
@@ -525,6 +526,10 @@ int sister_tune_set(sister_ctx *c, int key, int value) {
         c->tune_cs = value;
         break;
     case SISTER_TUNE_FULL_DISP: c->full_disp = value != 0; return SISTER_OK;
+    case SISTER_TUNE_WAIT_LIMIT_US:
+        if (value < 0) return c->fail(SISTER_EINVAL, "wait limit must be >= 0 microseconds (0: default)");
+        c->wait_limit_us = value ? (unsigned)value : kDefaultWaitUs;
+        return SISTER_OK;
     default: return c->fail(SISTER_EINVAL, "unknown or read-only tuning key %d", key);
     }
     c->plan_w = c->plan_h = c->plan_dc = 0; // re-plan on next use
@@ -542,6 +547,7 @@ int sister_tune_get(sister_ctx *c, int key, int *value) {
     case SISTER_TUNE_SGM_GROUPS: *value = p.ngroups; break;
     case SISTER_TUNE_SGM_CLUSTERS: *value = p.nclusters; break;
     case SISTER_TUNE_FULL_DISP: *value = c->full_disp ? 1 : 0; break;
+    case SISTER_TUNE_WAIT_LIMIT_US: *value = (int)c->wait_limit_us; break;
     default: return c->fail(SISTER_EINVAL, "unknown tuning key %d", key);
     }
     return SISTER_OK;

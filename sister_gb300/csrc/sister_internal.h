@@ -33,6 +33,12 @@ inline size_t progress_bytes(size_t ncounters) { return ncounters * kProgressStr
 
 // Device-side error codes written by kernels with bounded waits.
 enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
+// Default limit of a device-side wait on another warp or CTA (microseconds); a context may lower it
+// (SISTER_TUNE_WAIT_LIMIT_US). Waits for a warp's own asynchronous copies in flight (before its barriers are
+// reused or the CTA exits) always use kDrainLimitUs: those copies complete by themselves within microseconds,
+// and they must have landed before the shared memory they write is reused.
+constexpr unsigned kDefaultWaitUs = 2000000;
+constexpr unsigned kDrainLimitUs = 2000000;
 
 // One rig's aggregation buffers (all device pointers).
 struct SgmRig {
@@ -82,10 +88,11 @@ void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaS
 void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4,
                      unsigned *rowflags = nullptr, unsigned epoch = 0);
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4,
-                   const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr);
+                   const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr,
+                   unsigned wait_limit_us = kDefaultWaitUs);
 // pair WTA of every frame and the eight medians in one launch (medians follow the rows through rowflags)
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
-                       unsigned epoch, unsigned *err, cudaStream_t st);
+                       unsigned epoch, unsigned *err, cudaStream_t st, unsigned wait_limit_us = kDefaultWaitUs);
 // two-view doStereo tail: LR-checked left map (-10 where rejected) and the right map, from frame 0's medians
 void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16_t *outR, cudaStream_t st);
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
@@ -98,13 +105,14 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 SgmPlan sgm_plan_gb300(const Geom &g); // the plan on a 152-SM GB300, without a device query
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
 // single rig: rig.nbands is filled from the plan; rig.progress is zeroed here
-cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st);
+cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
+                       unsigned wait_limit_us = kDefaultWaitUs);
 // several rigs of one d-stride class: rigs / items in device memory (progress counters already zeroed); grid
 // = min(nitems, resident CTAs)
 int sgm_rows_max(int dp, int device);
 int sgm_rows_gb300(int dp); // sgm_rows_max on a GB300, without a device query
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
-                             unsigned *err, int device, cudaStream_t st);
+                             unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us = kDefaultWaitUs);
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,

@@ -147,14 +147,15 @@ def _sensor_noise(rnd: _Rand, img: np.ndarray, sigma2x: int = 2) -> np.ndarray:
 
 
 def make_rig(w: int, h: int, dmin: int, dmax: int, seed: int, tiles: int = 10, bump: bool = False,
-             sigma_blur: float = 1.5):
+             sigma_blur: float = 1.5, native: bool = True):
     """Returns (views, disparity): views = [center, right, top, left, bottom] u8 h x w; disparity int.
 
     Uses the library's C port of this generator (sister_synth_rig, byte-identical) when the library is
-    built, else the numpy definition below."""
-    native = _make_rig_native(w, h, dmin, dmax, seed, tiles, bump, sigma_blur)
-    if native is not None:
-        return native
+    built and `native` is true, else the numpy definition below (native=False never loads the library)."""
+    if native:
+        r = _make_rig_native(w, h, dmin, dmax, seed, tiles, bump, sigma_blur)
+        if r is not None:
+            return r
     return make_rig_numpy(w, h, dmin, dmax, seed, tiles, bump, sigma_blur)
 
 
@@ -194,20 +195,20 @@ def make_rig_numpy(w: int, h: int, dmin: int, dmax: int, seed: int, tiles: int =
 
 # ---- the named workloads -------------------------------------------------------------------------
 
-def rig_c1(seed: int = 1):
+def rig_c1(seed: int = 1, native: bool = True):
     """640x480, maxdisp 192, 8-12 tiles with disparity 20-180."""
     rnd = _Rand(seed ^ 0x5151)
-    return make_rig(640, 480, 20, 180, seed, tiles=rnd.int1(8, 12)), 192
+    return make_rig(640, 480, 20, 180, seed, tiles=rnd.int1(8, 12), native=native), 192
 
 
-def rig_c2(seed: int = 2):
+def rig_c2(seed: int = 2, native: bool = True):
     """1920x1080, maxdisp 256, 16 tiles + quadratic bump, disparity 10-240."""
-    return make_rig(1920, 1080, 10, 240, seed, tiles=16, bump=True), 256
+    return make_rig(1920, 1080, 10, 240, seed, tiles=16, bump=True, native=native), 256
 
 
-def rig_c5(seed: int = 5):
+def rig_c5(seed: int = 5, native: bool = True):
     """Stress rig: 4096x3000, maxdisp 512, 32 tiles, disparity 20-500, sigma_blur 0.8."""
-    return make_rig(4096, 3000, 20, 500, seed, tiles=32, sigma_blur=0.8), 512
+    return make_rig(4096, 3000, 20, 500, seed, tiles=32, sigma_blur=0.8, native=native), 512
 
 
 def batch_shapes(n: int = 64, seed: int = 3):

@@ -1,11 +1,18 @@
 """Regenerate the golden fixtures from the reference's own compiled code (oracle/_ref).
 
-Run from the repository root on an x86-64 host that has the reference tree:
-    python tests/golden/make_golden.py [--c2] [--stereo-only]
+Run from the repository root on an x86-64 host that has the reference tree, passing its path:
+    python tests/golden/make_golden.py --reference PATH [--c2] [--stereo-only]
+    python tests/golden/make_golden.py --c5
 
 Every case stores the SHA-256 of its five input views (so a test first checks that the seeded
 generator reproduces the same bytes on the machine it runs on) and the reference outputs of the three
 modes of compute_disparities. Small cases also store the inputs themselves.
+
+--c5 writes the stress rig's fixture (4096x3000, max disparity 512, mode 0). The reference cannot run that rig
+(its nine full volumes take 190 GB and its WTARight_SSE overflows a stack buffer above 256 disparities,
+postprocess.cpp:193), so this fixture comes from the oracle's bounded-memory restatement
+(orc_compute_stream), which the other fixtures pin: it reproduces every reference-made fixture here bit for
+bit (tests/test_oracle.py). Needs about 24 GB of host memory and a few minutes.
 """
 from __future__ import annotations
 
@@ -71,7 +78,28 @@ def make_stereo(ref):
         print(name)
 
 
+def make_c5():
+    """The stress rig's fixture from the bounded-memory oracle (see the module docstring)."""
+    t0 = time.time()
+    (views, _), dc = synth.rig_c5(5)
+    port = oracle.Port()
+    out, pad = port.compute_stream(views, dc, 0, padded=True)
+    h, w = out.shape
+    d = pad[dc:dc + h, dc:dc + w]
+    assert np.array_equal(out, np.minimum(d.astype(np.int64) * 255, 65535).astype(np.uint16))
+    np.savez_compressed(os.path.join(HERE, "c5_4096x3000_dc512.npz"), dc=dc, seed=5, views_sha=views_sha(views),
+                        multi_sha=out_sha(out), multi_d=d.astype(np.uint16),
+                        source="oracle orc_compute_stream (mode 0), %d OpenMP threads" % port.num_threads())
+    print("c5 %.1fs" % (time.time() - t0))
+
+
 def main():
+    if "--c5" in sys.argv:
+        make_c5()
+        return
+    if "--reference" not in sys.argv:
+        sys.exit("pass --reference PATH (the reference project tree) or --c5")
+    os.environ["SISTER_REFERENCE"] = sys.argv[sys.argv.index("--reference") + 1]
     ref = oracle.Ref()
     t0 = time.time()
     make_stereo(ref)

@@ -98,3 +98,68 @@ int main(int argc, char **argv) {
 
     subprocess.check_call(cmd)
     assert subprocess.run([str(exe)], capture_output=True).returncode == 0
+
+
+FAKE_OPENCV = r"""
+// minimal stand-in for the few cv::Mat members include/sister_gb300.hpp uses (OpenCV is not installed here)
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <vector>
+#define CV_8U 0
+#define CV_16UC1 2
+namespace cv {
+struct Mat {
+    int rows = 0, cols = 0, type_ = CV_8U, ch = 1;
+    size_t step = 0;
+    std::shared_ptr<std::vector<uint8_t>> buf;
+    Mat() = default;
+    Mat(int r, int c, int t, int channels = 1) { create(r, c, t); ch = channels; step = (size_t)c * channels; buf->resize(step * r); }
+    void create(int r, int c, int t) {
+        rows = r; cols = c; type_ = t; ch = 1;
+        step = (size_t)c * (t == CV_16UC1 ? 2 : 1);
+        buf = std::make_shared<std::vector<uint8_t>>(step * r);
+    }
+    int depth() const { return type_; }
+    int channels() const { return ch; }
+    bool isContinuous() const { return true; }
+    template <class T> T *ptr() { return reinterpret_cast<T *>(buf->data()); }
+    template <class T> const T *ptr() const { return reinterpret_cast<const T *>(buf->data()); }
+};
+}
+"""
+
+
+def test_reference_caller_compiles_against_cpp_header(tmp_path):
+    """The calls of the reference's compute_disp.cpp:26-35 -- the global class name SisterMultiviewDisparities
+    constructed from five cv::Mat and compute_disparities(dispCount, multi, horiz, vert) into cv::Mat -- compile
+    and link unchanged against include/sister_gb300.hpp with SISTER_WITH_OPENCV (cv::Mat faked: no OpenCV here)."""
+    import subprocess
+
+    (tmp_path / "opencv2").mkdir()
+    (tmp_path / "opencv2" / "core.hpp").write_text(FAKE_OPENCV)
+    src = tmp_path / "caller.cpp"
+    src.write_text('''
+#define SISTER_WITH_OPENCV
+#include "sister_gb300.hpp"
+#include <cstdio>
+int main(int argc, char **argv) {
+    if (argc < 2) return 0;
+    cv::Mat center(48, 64, CV_8U, 3), right(48, 64, CV_8U, 3), top(48, 64, CV_8U, 3), left(48, 64, CV_8U, 3),
+        bottom(48, 64, CV_8U, 3);
+    int dispCount = 16;
+    try {
+        SisterMultiviewDisparities multiview(center, right, top, left, bottom);
+        cv::Mat result_horizontal, result_vertical, result_multiview;
+        multiview.compute_disparities(dispCount, result_multiview, result_horizontal, result_vertical);
+        std::printf("%d %d\\n", result_multiview.rows, result_multiview.cols);
+    } catch (const sister::Error &e) { std::printf("error %d\\n", e.code()); return 1; }
+    return 0;
+}
+''')
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(sister_gb300.LIB_PATH)
+    subprocess.check_call(["g++", "-std=c++17", "-I", str(tmp_path), "-I", os.path.join(ROOT, "include"), str(src),
+                           "-L", libdir, "-lsister_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)])
+    assert subprocess.run([str(exe)], capture_output=True).returncode == 0

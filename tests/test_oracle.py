@@ -44,6 +44,41 @@ def test_port_matches_golden_c1(port):
     assert out_sha(vert) == str(z["vert_sha"])
 
 
+@pytest.mark.parametrize("path", small_golden_files(), ids=os.path.basename)
+def test_stream_oracle_matches_golden_small(port, path):
+    """The bounded-memory restatement (orc_compute_stream, which made the 4096x3000/512 fixture) reproduces the
+    reference-made fixtures, every mode."""
+    views, dc, gold, _ = load_small(path)
+    for mode in range(3):
+        got = port.compute_stream(views, dc, mode)
+        assert np.array_equal(got, gold[mode]), "mode %d differs in %d px" % (mode, int((got != gold[mode]).sum()))
+
+
+@pytest.mark.slow
+def test_stream_oracle_matches_golden_c1(port):
+    z = np.load(os.path.join(GOLDEN, "c1_640x480_dc192.npz"))
+    (views, _), dc = synth.rig_c1(int(z["seed"]))
+    for mode, key in enumerate(("multi_sha", "horiz_sha", "vert_sha")):
+        assert out_sha(port.compute_stream(views, dc, mode)) == str(z[key])
+
+
+@pytest.mark.parametrize("w,h,dc", [(40, 32, 264), (64, 48, 96)])
+def test_stream_oracle_matches_full_oracle_wide(port, w, h, dc):
+    """Above 256 disparities (where the reference's WTARight_SSE overflows) the two restatements agree."""
+    rng = np.random.default_rng(w * h + dc)
+    views = [rng.integers(0, 256, (h, w), dtype=np.uint8) for _ in range(5)]
+    full = port.compute(views, dc)
+    for mode in range(3):
+        assert np.array_equal(port.compute_stream(views, dc, mode), full[mode])
+
+
+def test_generator_reproduces_c5_inputs():
+    z = np.load(os.path.join(GOLDEN, "c5_4096x3000_dc512.npz"))
+    (views, _), dc = synth.rig_c5(int(z["seed"]))
+    assert dc == int(z["dc"])
+    assert views_sha(views) == str(z["views_sha"])
+
+
 def test_synthetic_scene_is_recovered(port):
     """The generator warps in the direction the matcher searches: disparities come back."""
     views, gt = synth.make_rig(160, 120, 4, 40, seed=7, tiles=4)
