@@ -132,14 +132,14 @@ def replica_value(world: int, steps: int, units_per_rig: float, seconds: float) 
     return world * steps * units_per_rig / seconds
 
 
-def make_rig():
+def make_rig(native: bool = True):
     from sister_gb300 import synth
 
     if (W_, H_, DC) == (1920, 1080, 256):
-        (views, _), dc = synth.rig_c2(SEED)
+        (views, _), dc = synth.rig_c2(SEED, native=native)
         return views, dc
     # other sizes (profiling runs): same generator family, disparities within [10, dc-16]
-    views, _ = synth.make_rig(W_, H_, 10, max(DC - 16, 12), seed=SEED, tiles=16, bump=True)
+    views, _ = synth.make_rig(W_, H_, 10, max(DC - 16, 12), seed=SEED, tiles=16, bump=True, native=native)
     return views, DC
 
 
@@ -167,10 +167,20 @@ def cpu_baseline_c2(views, dc):
             "sample": "one full 1920x1080/256 rig, mode 0, oracle C restatement (OpenMP), %.1f s" % t}
 
 
+def _pinned_u8(a):
+    """A pinned (page-locked) host copy of a u8 array, as a numpy view."""
+    import numpy as np
+    import torch
+
+    t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    return t.numpy(), t
+
+
 def batched_leg(local):
-    """C3: 64 uneven rigs (synth.batch_shapes(64, seed=3), mode 0) through sister_batch_run against the same
-    rigs as 64 sequential plain calls (one context, load views + compute per rig); host arrays in and out
-    for both, bit-exact comparison of every output."""
+    """C3: 64 uneven rigs (synth.batch_shapes(64, seed=3), mode 0) through sister_batch_run (continuous admission,
+    each rig on its own stream, overlapping) against the same rigs as 64 sequential plain calls (one context,
+    load views + compute per rig). Both arms read pinned host views and write host outputs; every output of the
+    batch is compared with the plain call's bit for bit."""
     import numpy as np
     import torch
     from concurrent.futures import ThreadPoolExecutor
@@ -180,14 +190,24 @@ def batched_leg(local):
     shapes = synth.batch_shapes(64, seed=3)
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         rigs = list(ex.map(lambda k: synth.rig_for_shape(*shapes[k], seed=1000 + k), range(len(shapes))))
+    keep = []
+    pinned = []
+    for (views, _), dc in rigs:
+        pv = []
+        for v in views:
+            a, t = _pinned_u8(v)
+            keep.append(t)
+            pv.append(a)
+        pinned.append((pv, dc))
     units = sum(w * h * dc for w, h, dc in shapes) / 1e9
     free, _ = torch.cuda.mem_get_info(local)
     budget = int(min(free - (48 << 30), 200 << 30))
     batch = sg.Batch(local, budget)
-    brigs = [(views, dc, (True, False, False)) for (views, _), dc in rigs]
-    got = batch.run(brigs)  # warm-up
+    brigs = [(views, dc, (True, False, False)) for views, dc in pinned]
+    got = batch.run(brigs)  # warm-up (pool growth, staging)
     times = []
-    for _ in range(2):
+    for _ in range(3):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         got = batch.run(brigs)
         times.append(time.perf_counter() - t0)
@@ -195,44 +215,70 @@ def batched_leg(local):
     t_batch = min(times)
     ctx = sg.Context(local)
     big = max(range(len(shapes)), key=lambda k: shapes[k][0] * shapes[k][1] * shapes[k][2])
-    ctx.load_views(rigs[big][0][0])
-    ctx.set_max_disparity(rigs[big][1])
+    ctx.load_views(pinned[big][0])
+    ctx.set_max_disparity(pinned[big][1])
     ctx.compute(True, False, False)  # buffers sized for the largest rig before timing
     match = True
-    t0 = time.perf_counter()
-    for k, ((views, _), dc) in enumerate(rigs):
-        ctx.load_views(views)
-        ctx.set_max_disparity(dc)
-        m = ctx.compute(True, False, False)[0]
+    plain = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outs = []
+        for views, dc in pinned:
+            ctx.load_views(views)
+            ctx.set_max_disparity(dc)
+            outs.append(ctx.compute(True, False, False)[0])
+        plain.append(time.perf_counter() - t0)
+    for k, m in enumerate(outs):
         match = match and bool(np.array_equal(m, got[k][0]))
-    t_plain = time.perf_counter() - t0
     ctx.close()
+    t_plain = min(plain)
     return {"workload": "64 uneven rigs: w~U[320,2448], h~U[240,2048] (x16), dc in {64,128,192,256} <= w/4, mode 0, "
-                        "seeds 1000..1063; host arrays in/out",
+                        "seeds 1000..1063; pinned host views in, host outputs",
             "rigs": len(shapes), "gpix_disp": units, "batched_value": units / t_batch, "batched_s": t_batch,
             "plain_value": units / t_plain, "plain_s": t_plain, "ratio": t_plain / t_batch,
-            "budget_gb": budget / 2**30, "outputs_match": match, "unit": UNIT}
+            "budget_gb": budget / 2**30, "outputs_match": match, "unit": UNIT,
+            "engine": "continuous admission, 8 rigs in flight, one stream each"}
 
 
-def served_leg(local, rates=(10.0, 25.0, 50.0), seconds=2.0):
+def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 2000.0), seconds=2.0,
+               max_queue=32):
     """C4: Poisson arrivals of single-rig requests (mix: 50% 640x480/128, 35% 1920x1080/256, 15% 2448x2048/256)
-    into the serving loop with a 16 GB device budget; latency = submission to outputs in host memory."""
+    into the serving loop with a 16 GB device budget and continuous admission; requests beyond a queue of
+    `max_queue` are refused (backpressure). Latency = submission to outputs in host memory (pinned views and
+    outputs). Per offered rate: accepted and refused requests, completed throughput, p50/p99 per class."""
     import numpy as np
     import random
+    import torch
     import sister_gb300 as sg
     from sister_gb300 import synth
 
     mix = synth.SERVE_MIX  # ((p, w, h, dc), ...)
-    pools = []
+    pools, keep = [], []
     for ci, (_, w, h, dc) in enumerate(mix):
         n = 4 if w * h < 1e6 else 2
-        pools.append([(synth.rig_for_shape(w, h, dc, seed=2000 + 10 * ci + k)[0][0], dc) for k in range(n)])
-    srv = sg.Server(local, 16 << 30)
-    # warm-up: one of each class
-    for ci in range(len(mix)):
-        srv.wait(srv.submit(pools[ci][0][0], mix[ci][3]))
+        pool = []
+        for k in range(n):
+            views = synth.rig_for_shape(w, h, dc, seed=2000 + 10 * ci + k)[0][0]
+            pv = []
+            for v in views:
+                a, t = _pinned_u8(v)
+                keep.append(t)
+                pv.append(a)
+            pool.append(pv)
+        outs = []
+        for _ in range(max_queue + 24):
+            t = torch.empty((h, w), dtype=torch.int16).pin_memory()
+            keep.append(t)
+            outs.append(t.numpy().view(np.uint16))
+        pools.append((pool, dc, outs))
+    srv = sg.Server(local, 16 << 30, max_inflight=8, max_queue=max_queue)
+    for ci in range(len(mix)):  # warm-up: one of each class
+        pool, dc, outs = pools[ci]
+        srv.wait(srv.submit(pool[0], dc, outputs=(outs[0],)))
     out = {"workload": "Poisson arrivals, mix 50%% 640x480/128, 35%% 1920x1080/256, 15%% 2448x2048/256, mode 0, "
-                       "16 GB device budget, dynamic batching; %.0f s per rate" % seconds, "unit": "ms", "rates": []}
+                       "16 GB device budget, continuous admission (8 in flight), queue bound %d; %.0f s per rate"
+                       % (max_queue, seconds), "unit": "ms", "rates": []}
     rnd = random.Random(7)
     for rate in rates:
         sched = []
@@ -244,29 +290,44 @@ def served_leg(local, rates=(10.0, 25.0, 50.0), seconds=2.0):
             u = rnd.random()
             ci = 0 if u < mix[0][0] else (1 if u < mix[0][0] + mix[1][0] else 2)
             sched.append((t, ci))
-        b0 = srv.stats()
-        tickets = []
+        s0 = srv.stats()
+        tickets, refused = [], [0, 0, 0]
+        nsub = [0, 0, 0]
         t0 = time.perf_counter()
         for (ta, ci) in sched:
             dt = ta - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            views, dc = pools[ci][len(tickets) % len(pools[ci])]
-            tickets.append((srv.submit(views, dc), ci))
+            pool, dc, outs = pools[ci]
+            k = nsub[ci]
+            nsub[ci] += 1
+            try:
+                tickets.append((srv.submit(pool[k % len(pool)], dc, outputs=(outs[k % len(outs)],)), ci))
+            except sg.SisterError as e:
+                if e.code != sg.SISTER_EBUSY:
+                    raise
+                refused[ci] += 1
         lat = [[], [], []]
         for tk, ci in tickets:
             lat[ci].append(srv.wait(tk, 120000)[1])
         span = time.perf_counter() - t0
-        b1 = srv.stats()
+        s1 = srv.stats()
         allv = sorted(x for l in lat for x in l)
         pct = lambda v, q: float(np.percentile(v, q)) if v else None
-        units = sum(mix[ci][1] * mix[ci][2] * mix[ci][3] for _, ci in sched) / 1e9
+        units = sum(mix[ci][1] * mix[ci][2] * mix[ci][3] for _, ci in tickets) / 1e9
         out["rates"].append({
-            "arrivals_per_s": rate, "requests": len(allv), "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+            "offered_per_s": rate, "submitted": len(sched), "accepted": len(tickets), "refused": sum(refused),
+            "completed_per_s": len(tickets) / span, "served_gpix_disp_per_s": units / span,
+            "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+            "p50_640x480_ms": pct(lat[0], 50), "p99_640x480_ms": pct(lat[0], 99),
             "p50_1080p_ms": pct(lat[1], 50), "p99_1080p_ms": pct(lat[1], 99),
-            "p99_640x480_ms": pct(lat[0], 99), "p99_2448x2048_ms": pct(lat[2], 99),
-            "served_gpix_disp_per_s": units / span, "batches": b1["batches"] - b0["batches"]})
+            "p50_2448x2048_ms": pct(lat[2], 50), "p99_2448x2048_ms": pct(lat[2], 99),
+            "peak_inflight": s1["peak_inflight"]})
     srv.close()
+    # the knee: the highest offered rate served without refusals and with the 1080p p99 under 20 ms
+    ok = [r["offered_per_s"] for r in out["rates"] if r["refused"] == 0 and (r["p99_1080p_ms"] or 0) < 20.0]
+    out["knee_offered_per_s"] = max(ok) if ok else None
+    out["max_completed_per_s"] = max(r["completed_per_s"] for r in out["rates"])
     return out
 
 
@@ -434,8 +495,8 @@ def run_reference(args):
     port = oracle.Port()
     full_cells = (W_ + 2 * DC) * (H_ + 2 * DC) * DC
 
-    def rig(w, h):
-        return synth.make_rig(w, h, 10, 240, seed=SEED, tiles=16, bump=True)[0]
+    def rig(w, h):  # numpy generator: this arm never loads the product library
+        return synth.make_rig(w, h, 10, 240, seed=SEED, tiles=16, bump=True, native=False)[0]
 
     # calibrate on a small rig, then pick the largest sample that keeps the run within ~3 minutes
     cal = rig(640, 360)
@@ -449,7 +510,7 @@ def run_reference(args):
             choice = cand
             break
     sw, sh = choice
-    views = rig(sw, sh) if choice != (W_, H_) else make_rig()[0]
+    views = rig(sw, sh) if choice != (W_, H_) else make_rig(native=False)[0]
     cells = (sw + 2 * DC) * (sh + 2 * DC) * DC
     for _ in range(args.warmup):
         port.compute(views, DC, modes=(True, False, False))

@@ -39,7 +39,9 @@ enum {
     SISTER_EBUDGET = -3,  /* request exceeds the configured HBM budget (serving) */
     SISTER_EDEVICE = -4,  /* CUDA error */
     SISTER_ETIMEOUT = -5, /* a bounded device-side wait expired */
-    SISTER_ESTATE = -6    /* call order violated (e.g. compute before load) */
+    SISTER_ESTATE = -6,   /* call order violated (e.g. compute before load) */
+    SISTER_EBUSY = -7,    /* serving: the request queue is full; nothing was queued (retry later) */
+    SISTER_EPENDING = -8  /* serving: the request is still queued or running (the ticket stays valid) */
 };
 
 typedef struct sister_ctx sister_ctx;
@@ -157,34 +159,46 @@ typedef struct sister_rig {
     uint16_t *multi, *horiz, *vert; /* host outputs, width*height u16 each (disparity*255); NULL skips a mode */
 } sister_rig;
 typedef struct sister_batch sister_batch;
-/* budget_bytes: device memory the engine may hold, allocated here as one arena (0: three quarters of the
- * device's free memory). */
+/* budget_bytes: device memory the rigs in flight may hold together (0: three quarters of the device's free
+ * memory), drawn from a pool owned by the batch. */
 SISTER_API int sister_batch_create(sister_batch **out, int device, size_t budget_bytes);
 SISTER_API void sister_batch_destroy(sister_batch *batch);
 SISTER_API const char *sister_batch_last_error(sister_batch *batch);
-/* Computes every rig and returns when all outputs are written. Rigs run in waves whose device memory fits
- * the budget; within a wave the stages before the aggregation run per rig on several streams and one
- * aggregation launch per disparity-stride class covers all of the wave's rigs. A rig that alone exceeds
- * the budget fails the call with SISTER_EBUDGET (nothing of the call has run). */
+/* Computes every rig and returns when all outputs are written. Rigs are admitted continuously: each starts as
+ * soon as a stream slot is free and its device memory fits the budget beside the rigs still running, and runs
+ * the whole pipeline on its own stream, overlapping the others. A bad rig, or one that alone exceeds the budget,
+ * fails the call (SISTER_EINVAL / SISTER_EBUDGET) before anything runs. Pinned (page-locked) host views and
+ * outputs are used in place; pageable ones go through pinned staging. */
 SISTER_API int sister_batch_run(sister_batch *batch, const sister_rig *rigs, int nrigs);
-/* Device bytes one rig takes inside a batch when nmodes of its outputs are requested. */
+/* Device bytes one rig holds while it is computed when nmodes of its outputs are requested (the modes share
+ * the aggregation volumes; BGR input counted). */
 SISTER_API size_t sister_batch_rig_bytes(int width, int height, int max_disparity, int nmodes);
 
 /* --- serving loop ------------------------------------------------------------------------------------
  * Requests (one rig each: dispCount + five images -> disparity images, the request shape of the reference's
- * ROS service recipe, ros/README.md:6-15) are submitted from any host thread; a worker thread drains the
- * queue into dynamic batches that fit the budget (sister_batch_run), in arrival order. The rig's views and
- * outputs must stay valid until sister_server_wait returns for its ticket. */
+ * ROS service recipe, ros/README.md:6-15) are submitted from any host thread and served with continuous
+ * admission: a request starts as soon as a stream slot is free and its device memory fits the budget beside the
+ * requests already running (in arrival order), its stages overlap theirs on the device, and its ticket completes
+ * when its own outputs are in host memory. The rig's views and outputs must stay valid until sister_server_wait
+ * returns for its ticket. */
 typedef struct sister_server sister_server;
 SISTER_API int sister_server_create(sister_server **out, int device, size_t budget_bytes);
-SISTER_API void sister_server_destroy(sister_server *server); /* finishes queued requests first */
+SISTER_API void sister_server_destroy(sister_server *server); /* finishes admitted and queued requests first */
+/* Message of the last failure; the string belongs to the calling thread until its next call. */
 SISTER_API const char *sister_server_last_error(sister_server *server);
-/* SISTER_EBUDGET if the rig alone exceeds the budget (nothing queued) */
+/* Requests computed at once (1..16, default 8) and requests waiting for admission (default 1024). */
+SISTER_API int sister_server_set_limits(sister_server *server, int max_inflight, size_t max_queue);
+/* SISTER_EBUDGET if the rig alone exceeds the budget, SISTER_EBUSY if the queue is full (backpressure),
+ * SISTER_EINVAL for a bad rig; nothing is queued then. */
 SISTER_API int sister_server_submit(sister_server *server, const sister_rig *rig, uint64_t *ticket);
-/* Blocks up to timeout_ms for the request; returns its status (SISTER_ETIMEOUT if still running) and its
- * latency from submission to outputs in host memory. */
+/* Blocks up to timeout_ms. Returns the request's status once its outputs are in host memory (the ticket is
+ * then released; SISTER_ETIMEOUT means a device-side wait of that request expired) or SISTER_EPENDING if it is
+ * still queued or running (the ticket stays valid). latency_ms: submission to outputs in host memory. Finished
+ * tickets that are never waited for are dropped after 4096 later completions. */
 SISTER_API int sister_server_wait(sister_server *server, uint64_t ticket, int timeout_ms, double *latency_ms);
-SISTER_API int sister_server_stats(sister_server *server, uint64_t *batches, uint64_t *rigs);
+/* Counters: requests admitted, completed, refused for a full queue, and the most requests in flight at once. */
+SISTER_API int sister_server_stats(sister_server *server, uint64_t *admitted, uint64_t *completed, uint64_t *rejected,
+                                   int *peak_inflight);
 
 /* --- synthetic workloads ------------------------------------------------------------------------------
  * Seeded synthetic rig (no dataset ships with the reference): views = 5 x h x w u8 (center, right, top,

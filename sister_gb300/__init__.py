@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsister_g
 
 SISTER_OK = 0
 SISTER_EINVAL, SISTER_ENOMEM, SISTER_EBUDGET, SISTER_EDEVICE, SISTER_ETIMEOUT, SISTER_ESTATE = -1, -2, -3, -4, -5, -6
+SISTER_EBUSY, SISTER_EPENDING = -7, -8
 _ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
 
 STAGES = {1: "frames", 2: "census", 3: "pair_wta", 4: "median", 5: "masks", 6: "cost", 7: "aggregate", 8: "wta"}
@@ -93,7 +94,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.sister_server_last_error.restype = ctypes.c_char_p
     lib.sister_server_submit.argtypes = [_vp, ctypes.POINTER(SisterRig), ctypes.POINTER(ctypes.c_uint64)]
     lib.sister_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-    lib.sister_server_stats.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    lib.sister_server_stats.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                        ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]
+    lib.sister_server_set_limits.argtypes = [_vp, ctypes.c_int, ctypes.c_size_t]
     if path is None:
         _lib = lib
     return lib
@@ -305,14 +308,21 @@ class Batch:
         return outs
 
 
-def _fill_rig(r, views, dc, modes):
+def _fill_rig(r, views, dc, modes, outputs=None):
     vs = _as_views(views)
     h, w = vs[0].shape[:2]
     ch = 1 if vs[0].ndim == 2 else 3
     for v in range(5):
         r.views[v] = vs[v].ctypes.data
     r.width, r.height, r.stride, r.channels, r.max_disparity = w, h, w * ch, ch, int(dc)
-    o = tuple(np.empty((h, w), np.uint16) if m else None for m in modes)
+    if outputs is not None:
+        it = iter(outputs)
+        o = tuple(next(it) if m else None for m in modes)
+        for a in o:
+            if a is not None and (a.dtype != np.uint16 or a.shape != (h, w) or not a.flags["C_CONTIGUOUS"]):
+                raise ValueError("outputs must be C-contiguous uint16 arrays of shape %s" % ((h, w),))
+    else:
+        o = tuple(np.empty((h, w), np.uint16) if m else None for m in modes)
     r.multi = o[0].ctypes.data if o[0] is not None else None
     r.horiz = o[1].ctypes.data if o[1] is not None else None
     r.vert = o[2].ctypes.data if o[2] is not None else None
@@ -321,9 +331,11 @@ def _fill_rig(r, views, dc, modes):
 
 class Server:
     """Serving loop (sister_server): submit(views, dispCount[, modes]) from any thread returns a ticket;
-    wait(ticket) returns (outputs, latency_ms). Requests are computed in dynamic batches within the budget."""
+    wait(ticket) returns (outputs, latency_ms). Requests are admitted continuously as stream slots and device
+    memory free up, run concurrently on the device, and complete one by one."""
 
-    def __init__(self, device: int = 0, budget_bytes: int = 16 << 30):
+    def __init__(self, device: int = 0, budget_bytes: int = 16 << 30, max_inflight: int | None = None,
+                 max_queue: int | None = None):
         self.lib = load_library()
         h = ctypes.c_void_p()
         rc = self.lib.sister_server_create(ctypes.byref(h), int(device), int(budget_bytes))
@@ -331,31 +343,43 @@ class Server:
             raise SisterError(rc, "sister_server_create(device=%d, budget=%d) failed" % (device, budget_bytes))
         self.h = h
         self._live = {}
+        if max_inflight is not None or max_queue is not None:
+            self.set_limits(max_inflight or 8, max_queue if max_queue is not None else 1024)
 
-    def submit(self, views, dc, modes=(True, False, False)) -> int:
+    def set_limits(self, max_inflight: int, max_queue: int):
+        rc = self.lib.sister_server_set_limits(self.h, int(max_inflight), ctypes.c_size_t(int(max_queue)))
+        if rc != SISTER_OK:
+            raise SisterError(rc, "sister_server_set_limits failed")
+
+    def _err(self) -> str:
+        return self.lib.sister_server_last_error(self.h).decode(errors="replace")
+
+    def submit(self, views, dc, modes=(True, False, False), outputs=None) -> int:
+        """outputs: optional tuple of caller-owned u16 h x w arrays (e.g. in pinned memory) per requested mode."""
         r = SisterRig()
-        vs, o = _fill_rig(r, views, dc, modes)
+        vs, o = _fill_rig(r, views, dc, modes, outputs)
         t = ctypes.c_uint64(0)
         rc = self.lib.sister_server_submit(self.h, ctypes.byref(r), ctypes.byref(t))
         if rc != SISTER_OK:
-            raise SisterError(rc, "sister_server_submit failed")
+            raise SisterError(rc, self._err())
         self._live[t.value] = (vs, o)
         return t.value
 
     def wait(self, ticket: int, timeout_ms: int = 60000):
         lat = ctypes.c_double(0)
         rc = self.lib.sister_server_wait(self.h, ticket, int(timeout_ms), ctypes.byref(lat))
-        if rc == SISTER_ETIMEOUT:
-            raise TimeoutError("request %d still running after %d ms" % (ticket, timeout_ms))
+        if rc == SISTER_EPENDING:
+            raise TimeoutError("request %d still queued or running after %d ms" % (ticket, timeout_ms))
         vs, o = self._live.pop(ticket)
         if rc != SISTER_OK:
-            raise SisterError(rc, self.lib.sister_server_last_error(self.h).decode(errors="replace"))
+            raise SisterError(rc, self._err())
         return o, lat.value
 
     def stats(self):
-        b, r = ctypes.c_uint64(0), ctypes.c_uint64(0)
-        self.lib.sister_server_stats(self.h, ctypes.byref(b), ctypes.byref(r))
-        return {"batches": b.value, "rigs": r.value}
+        a, c, r = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+        p = ctypes.c_int(0)
+        self.lib.sister_server_stats(self.h, ctypes.byref(a), ctypes.byref(c), ctypes.byref(r), ctypes.byref(p))
+        return {"admitted": a.value, "completed": c.value, "rejected": r.value, "peak_inflight": p.value}
 
     def close(self):
         if getattr(self, "h", None):

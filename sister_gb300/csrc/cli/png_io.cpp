@@ -8,66 +8,106 @@ namespace pngio {
 namespace {
 
 // ---------------------------------------------------------------- DEFLATE decoder (RFC 1951)
+// Bit reader: DEFLATE packs data LSB first. peek() looks at the next k bits (zero past the end of the input),
+// skip() consumes them and flags a read past the end.
 struct Bits {
     const uint8_t *p;
     size_t n, pos = 0;
-    uint32_t buf = 0;
+    uint64_t buf = 0;
     int cnt = 0;
     bool bad = false;
-    int need(int k) { // next k bits, LSB first
-        while (cnt < k) {
-            if (pos >= n) {
-                bad = true;
-                return 0;
-            }
-            buf |= (uint32_t)p[pos++] << cnt;
+    void fill() {
+        while (cnt <= 56 && pos < n) {
+            buf |= (uint64_t)p[pos++] << cnt;
             cnt += 8;
         }
-        const int v = (int)(buf & ((1u << k) - 1));
+    }
+    unsigned peek(int k) {
+        if (cnt < k) fill();
+        return (unsigned)(buf & ((1ull << k) - 1));
+    }
+    void skip(int k) {
+        if (cnt < k) fill();
+        if (cnt < k) {
+            bad = true;
+            buf = 0;
+            cnt = 0;
+            return;
+        }
         buf >>= k;
         cnt -= k;
-        return v;
+    }
+    int need(int k) { // the next k bits as a number, consumed
+        if (k == 0) return 0;
+        const int v = (int)peek(k);
+        skip(k);
+        return bad ? 0 : v;
+    }
+    size_t byte_end() const { return pos - (size_t)(cnt >> 3); } // first byte not touched by consumed bits
+    void align() { // drop the bits of the current byte (stored blocks start on a byte boundary)
+        const int drop = cnt & 7;
+        buf >>= drop;
+        cnt -= drop;
     }
 };
 
+// Huffman decoding by direct lookup: the table is indexed by the next kMaxBits input bits and holds, for
+// every index, the symbol whose (bit-reversed) canonical code is a prefix of those bits and the code's length.
+// Canonical codes follow RFC 1951 section 3.2.2: codes of each length are consecutive, shorter codes first,
+// in symbol order within a length.
+constexpr int kMaxBits = 15;
 struct Huff {
-    int count[16] = {};
-    int symbol[320] = {};
+    std::vector<uint32_t> table; // (symbol << 4) | length; 0 = no code (invalid input)
 };
 
-// canonical code from code lengths; returns false for an over-subscribed set
+unsigned reverse_bits(unsigned v, int len) {
+    unsigned r = 0;
+    for (int k = 0; k < len; k++) r |= ((v >> k) & 1u) << (len - 1 - k);
+    return r;
+}
+
+// false for an over-subscribed set of lengths (incomplete sets are accepted, as zlib does for one-code trees)
 bool build(Huff &h, const int *len, int n) {
-    std::memset(h.count, 0, sizeof h.count);
-    for (int s = 0; s < n; s++) h.count[len[s]]++;
-    h.count[0] = 0;
-    int left = 1;
-    for (int l = 1; l < 16; l++) {
-        left <<= 1;
-        left -= h.count[l];
-        if (left < 0) return false;
+    int count[kMaxBits + 1] = {};
+    for (int s = 0; s < n; s++) count[len[s]]++;
+    count[0] = 0;
+    long kraft = 0; // sum of 2^(kMaxBits - length)
+    for (int l = 1; l <= kMaxBits; l++) kraft += (long)count[l] << (kMaxBits - l);
+    if (kraft > (1L << kMaxBits)) return false;
+    unsigned next[kMaxBits + 2] = {};
+    unsigned code = 0;
+    for (int l = 1; l <= kMaxBits; l++) {
+        code = (code + count[l - 1]) << 1;
+        next[l] = code;
     }
-    int offs[16];
-    offs[1] = 0;
-    for (int l = 1; l < 15; l++) offs[l + 1] = offs[l] + h.count[l];
-    for (int s = 0; s < n; s++)
-        if (len[s]) h.symbol[offs[len[s]]++] = s;
+    h.table.assign(1u << kMaxBits, 0u);
+    for (int s = 0; s < n; s++) {
+        const int l = len[s];
+        if (!l) continue;
+        const unsigned r = reverse_bits(next[l]++, l);
+        for (unsigned hi = 0; hi < (1u << (kMaxBits - l)); hi++) h.table[r | (hi << l)] = (uint32_t)s << 4 | (uint32_t)l;
+    }
     return true;
 }
 
 int decode(Bits &b, const Huff &h) {
-    int code = 0, first = 0, index = 0;
-    for (int l = 1; l < 16; l++) {
-        code |= b.need(1);
-        if (b.bad) return -1;
-        const int c = h.count[l];
-        if (code - c < first) return h.symbol[index + (code - first)];
-        index += c;
-        first += c;
-        first <<= 1;
-        code <<= 1;
-    }
-    return -1;
+    const uint32_t e = h.table[b.peek(kMaxBits)];
+    if (!e) return -1;
+    b.skip((int)(e & 15u));
+    return b.bad ? -1 : (int)(e >> 4);
 }
+
+// the fixed codes of block type 1 (RFC 1951 section 3.2.6), built once (thread-safe static initialisation)
+struct FixedCodes {
+    Huff lit, dist;
+    FixedCodes() {
+        int l[288], d[30];
+        for (int s = 0; s < 288; s++) l[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
+        for (int s = 0; s < 30; s++) d[s] = 5;
+        build(lit, l, 288);
+        build(dist, d, 30);
+    }
+};
 
 const int kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27, 31, 35, 43, 51, 59, 67, 83, 99, 115, 131,
                           163, 195, 227, 258};
@@ -106,26 +146,17 @@ std::string inflate_raw(Bits &b, std::vector<uint8_t> &out) {
         const int type = b.need(2);
         if (b.bad) return "truncated stream";
         if (type == 0) {
-            b.buf = 0;
-            b.cnt = 0; // stored block: byte-aligned
-            if (b.pos + 4 > b.n) return "truncated stored block";
-            const unsigned len = b.p[b.pos] | (b.p[b.pos + 1] << 8), nlen = b.p[b.pos + 2] | (b.p[b.pos + 3] << 8);
-            b.pos += 4;
-            if ((len ^ 0xFFFFu) != nlen || b.pos + len > b.n) return "bad stored block";
-            out.insert(out.end(), b.p + b.pos, b.p + b.pos + len);
-            b.pos += len;
-        } else if (type == 1) {
-            static Huff lit, dist;
-            static bool ready = false;
-            if (!ready) {
-                int l[288], d[30];
-                for (int s = 0; s < 288; s++) l[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
-                for (int s = 0; s < 30; s++) d[s] = 5;
-                build(lit, l, 288);
-                build(dist, d, 30);
-                ready = true;
+            b.align(); // stored block: LEN and NLEN start at the next byte boundary
+            const unsigned len = (unsigned)b.need(16), nlen = (unsigned)b.need(16);
+            if (b.bad || (len ^ 0xFFFFu) != nlen) return "bad stored block";
+            for (unsigned k = 0; k < len; k++) {
+                const int v = b.need(8);
+                if (b.bad) return "truncated stored block";
+                out.push_back((uint8_t)v);
             }
-            const std::string e = codes(b, lit, dist, out);
+        } else if (type == 1) {
+            static const FixedCodes fixed;
+            const std::string e = codes(b, fixed.lit, fixed.dist, out);
             if (!e.empty()) return e;
         } else if (type == 2) {
             const int nlen = b.need(5) + 257, ndist = b.need(5) + 1, ncode = b.need(4) + 4;
@@ -168,19 +199,21 @@ std::string inflate_raw(Bits &b, std::vector<uint8_t> &out) {
 }
 
 // ---------------------------------------------------------------- checksums
-uint32_t crc32(const uint8_t *p, size_t n, uint32_t c = 0) {
-    static uint32_t table[256];
-    static bool ready = false;
-    if (!ready) {
+struct CrcTable {
+    uint32_t t[256];
+    CrcTable() {
         for (uint32_t k = 0; k < 256; k++) {
             uint32_t v = k;
             for (int j = 0; j < 8; j++) v = (v & 1) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
-            table[k] = v;
+            t[k] = v;
         }
-        ready = true;
     }
+};
+
+uint32_t crc32(const uint8_t *p, size_t n, uint32_t c = 0) {
+    static const CrcTable table; // built once, thread-safe static initialisation
     c = ~c;
-    for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xFF] ^ (c >> 8);
+    for (size_t i = 0; i < n; i++) c = table.t[(c ^ p[i]) & 0xFF] ^ (c >> 8);
     return ~c;
 }
 
@@ -212,7 +245,7 @@ std::string zlib_inflate(const uint8_t *data, size_t n, std::vector<uint8_t> &ou
     Bits b{data + 2, n - 2};
     std::string e = inflate_raw(b, out);
     if (!e.empty()) return e;
-    const size_t end = b.pos; // the remaining bits of the last byte are padding
+    const size_t end = b.byte_end(); // the remaining bits of the last byte are padding
     if (end + 4 > b.n) return "missing adler32";
     if (be32(b.p + end) != adler32(out.data(), out.size())) return "adler32 mismatch";
     return "";

@@ -9,7 +9,7 @@
 // coupled only through the per-pixel sum.
 //
 // The two passes are independent until their sums meet, so one persistent launch runs the bands of both
-// interleaved (work item k: pass k & 1, band k >> 1); each pass stores its 4-path sum and a final
+// interleaved (work item k: pass k & 1, band k >> 1, drawn by the CTAs from a ticket); each pass stores its 4-path sum and a final
 // memory-bound kernel adds the two sums and takes the winner-take-all. While the bands of one pass wait
 // on the wavefront above them, the other pass's bands keep the SMs busy.
 //
@@ -255,7 +255,6 @@ __device__ __forceinline__ void stg_stream(uint16_t *p, const uint32_t (&v)[NP])
 
 // ---------------------------------------------------------------- packed path update
 __device__ __forceinline__ uint32_t perm_hi_lo(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
-__device__ __forceinline__ uint32_t hmin(uint32_t v) { return min(v & 0xFFFFu, v >> 16); }
 // the smaller half of v in both halves: a warp minimum of such pairs is again a pair (m, m)
 __device__ __forceinline__ uint32_t hmin2(uint32_t v) { return __vminu2(v, __byte_perm(v, 0, 0x1032)); }
 
@@ -334,8 +333,16 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     auto hend = [&](int b) { return min(W, hstart(b + 1)); };
     auto hbatch = [&](int x) { return x < HB ? (x < 2 ? 0 : 31 - __clz(x)) : x / HB + NPF - 1; };
 
+    // Work items are drawn from a ticket in item order, so every item a CTA waits on (the previous band of its
+    // pass) was drawn earlier by a CTA that is running or done: the launch completes however many of its CTAs
+    // are resident, and needs no cooperative launch -- other kernels may share the GPU with it.
+    __shared__ int s_item;
     bool first_band = true;
-    for (int item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(a.claim, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.nitems) break;
         int band;
         SgmRig rg;
         if (a.items) {
@@ -807,7 +814,7 @@ SgmPlan plan_rows(const Geom &g, int sms, int lo, int hi, F per_sm) {
             p.R = R;
             p.nbands = nb;
             p.ngroups = items;
-            p.nclusters = conc; // persistent CTAs, all co-resident
+            p.nclusters = conc; // persistent CTAs (the grid)
         }
     }
     p.cs = p.R ? 1 : 0;
@@ -865,19 +872,19 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
     a.nitems = p.ngroups;
     a.R = p.R;
     a.dp = g.dp;
+    a.claim = rig.progress + (size_t)p.ngroups * kProgressStride;
     a.err = err;
     a.wait_limit_us = wait_limit_us;
-    cudaError_t e = cudaMemsetAsync(rig.progress, 0, progress_bytes(p.ngroups), st);
+    cudaError_t e = cudaMemsetAsync(rig.progress, 0, sgm_progress_bytes(p.ngroups), st);
     if (e != cudaSuccess) return e;
     void *args[] = {(void *)&a};
-    // cooperative launch: every CTA is resident, and each work item depends only on work items of lower
-    // index (the previous band of its pass), so no item waits on one that cannot run
-    return cudaLaunchCooperativeKernel(fn, dim3(p.nclusters), dim3((p.R + kHelpers) * 32), args,
-                                       sgm_smem(p.R, g.dp).total, st);
+    // each work item depends only on items drawn before it (the previous band of its pass), so a plain launch
+    // of any grid size completes
+    return cudaLaunchKernel(fn, dim3(p.nclusters), dim3((p.R + kHelpers) * 32), args, sgm_smem(p.R, g.dp).total, st);
 }
 
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
-                             unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us) {
+                             unsigned *claim, unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us) {
     const int dpl = dp / 32;
     const void *fn = kernel_for(dpl);
     if (!fn || R < 1 || nitems < 1) return cudaErrorInvalidValue;
@@ -895,11 +902,12 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
     a.nitems = nitems;
     a.R = R;
     a.dp = dp;
+    a.claim = claim;
     a.err = err;
     a.wait_limit_us = wait_limit_us;
     void *args[] = {(void *)&a};
-    return cudaLaunchCooperativeKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R + kHelpers) * 32), args,
-                                       sgm_smem(R, dp).total, st);
+    return cudaLaunchKernel(fn, dim3(std::min(nitems, per_sm * sms)), dim3((R + kHelpers) * 32), args,
+                            sgm_smem(R, dp).total, st);
 }
 
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,

@@ -90,7 +90,7 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     if (p.R < 1) return report(err, errlen, SISTER_EDEVICE, "no launch configuration fits the aggregation kernel");
     const size_t sum_bytes = align256(g.plane * g.dp * sizeof(uint16_t));
     const size_t bnd_bytes = align256(sgm_bnd_bytes(g, p));
-    const size_t prog_bytes = align256(progress_bytes(p.ngroups));
+    const size_t prog_bytes = align256(sgm_progress_bytes(p.ngroups));
     const size_t need = 2 * sum_bytes + bnd_bytes + prog_bytes + 256;
     if (need > kStaticScratchBytes) {
         char buf[256];

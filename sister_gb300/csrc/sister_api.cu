@@ -189,7 +189,7 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
         {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
         {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
-        {&c->progress, progress_bytes(std::max(p.ngroups, 1)), "progress"},
+        {&c->progress, sgm_progress_bytes(std::max(p.ngroups, 1)), "progress"},
         {&c->errflag, sizeof(unsigned), "error flag"},
         {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
         {&c->outs, 3 * (size_t)g.w * g.h * sizeof(uint16_t), "outputs"},
@@ -404,7 +404,7 @@ int sister_stereo(sister_ctx *c, const uint8_t *center, const uint8_t *other, in
         {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
         {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
         {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
-        {&c->progress, progress_bytes(std::max(p.ngroups, 1)), "progress"},
+        {&c->progress, sgm_progress_bytes(std::max(p.ngroups, 1)), "progress"},
         {&c->outs, 2 * plane * sizeof(uint16_t), "outputs"},
     };
     for (auto &r : req) {
@@ -485,7 +485,7 @@ size_t sister_device_bytes(int width, int height, int dc) {
     const size_t nbands = (size_t)p.nbands;
     const size_t bnd = 2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2;
     return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 3 * vol * 2 +
-           bnd + progress_bytes(2 * nbands) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+           bnd + sgm_progress_bytes(2 * nbands) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
 }
 
 int sister_profile_enable(sister_ctx *c, int on) {

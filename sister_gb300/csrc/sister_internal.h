@@ -30,6 +30,9 @@ Geom make_geom(int w, int h, int dc);
 // while the writer updates it, and neighbouring bands' counters must not share the line.
 constexpr int kProgressStride = 32;
 inline size_t progress_bytes(size_t ncounters) { return ncounters * kProgressStride * sizeof(unsigned); }
+// progress counters of an aggregation launch with `nitems` work items, plus one more line for the launch's item
+// ticket (the counter CTAs draw their next work item from)
+inline size_t sgm_progress_bytes(size_t nitems) { return progress_bytes(nitems + 1); }
 
 // Device-side error codes written by kernels with bounded waits.
 enum : unsigned { kErrNone = 0, kErrTimeout = 1 };
@@ -61,6 +64,7 @@ struct SgmLaunch {
                             // after the previous band of its rig and pass (multi-rig launch), or nullptr
     int nitems;
     int R, dp;              // rows per band (one warp per row + fetcher and writer per CTA); d-stride
+    unsigned *claim;        // item ticket, zero at launch: a CTA takes its next work item from an atomic add
     unsigned *err;          // device error flag
     unsigned wait_limit_us; // longest wait of any warp (microseconds) before reporting kErrTimeout
 };
@@ -104,15 +108,17 @@ void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 SgmPlan sgm_plan_gb300(const Geom &g); // the plan on a 152-SM GB300, without a device query
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
-// single rig: rig.nbands is filled from the plan; rig.progress is zeroed here
+// single rig: rig.nbands is filled from the plan; rig.progress (sgm_progress_bytes(p.ngroups): the counters and
+// the item ticket) is zeroed here
 cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
                        unsigned wait_limit_us = kDefaultWaitUs);
-// several rigs of one d-stride class: rigs / items in device memory (progress counters already zeroed); grid
-// = min(nitems, resident CTAs)
+// several rigs of one d-stride class: rigs / items in device memory (progress counters and the item ticket
+// `claim` already zeroed); grid = min(nitems, resident CTAs)
 int sgm_rows_max(int dp, int device);
 int sgm_rows_gb300(int dp); // sgm_rows_max on a GB300, without a device query
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
-                             unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us = kDefaultWaitUs);
+                             unsigned *claim, unsigned *err, int device, cudaStream_t st,
+                             unsigned wait_limit_us = kDefaultWaitUs);
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,

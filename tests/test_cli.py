@@ -22,7 +22,8 @@ def test_cli_selftest(cli):
     assert r.returncode == 0 and "selftest ok" in r.stdout
 
 
-@pytest.mark.parametrize("shape,level", [((37, 53), 1), ((64, 48), 9), ((31, 29, 3), 6), ((50, 70, 3), 0)])
+@pytest.mark.parametrize("shape,level", [((37, 53), 1), ((64, 48), 9), ((31, 29, 3), 6), ((50, 70, 3), 0),
+                                         ((300, 410), 9), ((120, 200, 3), 3)])
 def test_png_decoder_matches_zlib_written_images(cli, tmp_path, shape, level):
     rnd = np.random.default_rng(sum(shape) * 7 + level)
     # smooth + noisy content so the deflater emits both literal runs and matches
