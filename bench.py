@@ -46,6 +46,12 @@ KERNELS_PER_COMPUTE = 7
 # dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.817 + 1.110 GB for 992*832*256 cells. It exceeds
 # the 8 algorithmic bytes per cell by the band hand-off records; scaled to other rigs by the cell count.
 TRAFFIC_BYTES_PER_CELL = (0.816880640e9 + 1.109881e9) / (992 * 832 * 256)
+# integer operations of the algorithm per padded cell: masked 4-pair cost (popcounts, masks, selects, adds) ~36,
+# 8 aggregation paths x 8 (3 minima, saturating adds and subtraction, running minimum), the 8-path sum 7, pair WTA
+# (left and right) 8, final WTA 2 -- about 98 -- and the 32-bit popcounts among them: 8 for the cost and 8 for the
+# pair WTA
+INT_OPS_PER_CELL = 98
+POPC_PER_CELL = 16
 
 
 def rig_units() -> float:
@@ -141,6 +147,19 @@ def make_rig(native: bool = True):
     # other sizes (profiling runs): same generator family, disparities within [10, dc-16]
     views, _ = synth.make_rig(W_, H_, 10, max(DC - 16, 12), seed=SEED, tiles=16, bump=True, native=native)
     return views, DC
+
+
+def golden_modes():
+    """SHA-256 of the reference's three outputs for the 1920x1080/256 rig, or None for other rigs."""
+    import numpy as np
+
+    if (W_, H_, DC) != (1920, 1080, 256):
+        return None
+    try:
+        z = np.load(os.path.join(ROOT, "tests", "golden", "c2_1920x1080_dc256.npz"))
+        return [str(z[k]) for k in ("multi_sha", "horiz_sha", "vert_sha")]
+    except Exception:
+        return None
 
 
 def golden_sha():
@@ -440,21 +459,59 @@ def run_gb300(args):
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_ok = bool((pin_out.numpy().view(np.uint16) == got).all())
 
-    # roofline of the dominant kernel (the aggregation launch, both passes): algorithmic bytes per launch =
-    # per pass the cost volume read (2 B/cell) and the pass sum written (2 B/cell); cells = (w+2dc)(h+2dc)dc
+    # the reference's full call: compute_disparities with all three outputs (multiview, horizontal, vertical) on
+    # the same rig; the modes share the stages before the aggregation and are aggregated in one launch
+    modes3 = None
+    if not args.no_modes3:
+        outs3 = [torch.empty((h, w), dtype=torch.int16, device="cuda") for _ in range(3)]
+        ctx.load_views_device([t.data_ptr() for t in dev_views], w, h, w, 1)
+        ctx.compute_device(*[o.data_ptr() for o in outs3])
+        ctx.synchronize()
+        shas = golden_modes()
+        ok3 = all(hashlib.sha256(np.ascontiguousarray(o.cpu().numpy().view(np.uint16)).tobytes()).hexdigest() == sh
+                  for o, sh in zip(outs3, shas)) if shas else None
+        e3 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for a, b in e3:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a.record(stream)
+            ctx.compute_device(*[o.data_ptr() for o in outs3])
+            b.record(stream)
+        ctx.synchronize()
+        ms3 = min(a.elapsed_time(b) for a, b in e3)
+        modes3 = {"workload": "compute_disparities with all three outputs, 1920x1080/256 (modes 0, 1, 2)",
+                  "ms_per_call": ms3, "value": rig_units() / (ms3 / 1e3), "unit": UNIT + " (w*h*dc per call)",
+                  "outputs_per_s_value": 3 * rig_units() / (ms3 / 1e3), "bit_exact_vs_reference_golden": ok3}
+
+    # roofline of the dominant kernel (the aggregation launch, both passes), with the algorithmic bytes of the
+    # algorithm's aggregation: the u16 sum volume written once and read once, 4 B per padded cell (the launch's
+    # own traffic -- both passes read the cost volume and write their own sum -- is reported as `traffic`)
     cells = (w + 2 * dc) * (h + 2 * dc) * dc
     sgm = stage_ms.get("aggregate", [])
     peak, peak_kind = load_peaks()
     roof = None
+    step_ms = total_ms / args.steps
     if sgm:
         avg = sum(sgm) / len(sgm)
-        achieved = 8.0 * cells / (avg / 1e3) / 1e9
+        achieved = 4.0 * cells / (avg / 1e3) / 1e9
         roof = {"kernel": "sgm_kernel (8-path aggregation, both passes in one launch)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": TRAFFIC_BYTES_PER_CELL * cells,
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of sgm_kernel<8> on a 480x320/256 "
                                   "rig (1.93 GB for 211 M padded cells), scaled to this launch by the cell count",
-                "peak_source": peak_kind, "algorithmic_bytes_per_launch": 8 * cells, "launch_ms": avg}
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": 4 * cells, "launch_ms": avg}
+    # whole step against the integer roofline: 98 integer ops per padded cell (the algorithm's count), against the
+    # ALU pipe's 64 int32 lanes per clock per SM (ncu-derived) at the SM clock sampled during the timed region
+    clk_mhz = clk.get("sm_mhz") or 2070.0
+    int_peak = 152 * 64 * clk_mhz * 1e6
+    int_ops = INT_OPS_PER_CELL * cells
+    int_issue = {"ops_per_cell": INT_OPS_PER_CELL, "ops_per_step": int_ops, "achieved_tops": int_ops / (step_ms / 1e3) / 1e12,
+                 "peak_tops": int_peak / 1e12, "frac": int_ops / (step_ms / 1e3) / int_peak,
+                 "peak_source": "ncu: ALU pipe = 2.0 warp-instructions per SM-cycle (64 int32 lanes/clk/SM), x 152 SMs x "
+                                "the sampled SM clock (profiles/pipes_480x320x256.md)",
+                 "popc": {"per_cell": POPC_PER_CELL, "achieved_tops": POPC_PER_CELL * cells / (step_ms / 1e3) / 1e12,
+                          "peak_tops": 152 * 32 * clk_mhz * 1e6 / 1e12}}
 
     if rank == 0:
         line = {
@@ -466,7 +523,7 @@ def run_gb300(args):
                     "h2d_bytes_per_step": 5 * w * h, "d2h_bytes_per_step": 2 * w * h, "output_matches": e2e_ok},
             "gpu_launches": KERNELS_PER_COMPUTE * args.steps,
             "stage_ms_mean": {k: sum(v) / len(v) for k, v in stage_ms.items()},
-            "roofline": roof, "clocks": clk,
+            "roofline": roof, "int_issue": int_issue, "clocks": clk, "modes3": modes3,
         }
         if world == 1 and not args.no_batched:
             line["batched"] = batched_leg(local)
@@ -546,6 +603,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-rig batched-vs-plain leg")
     ap.add_argument("--no-served", action="store_true", help="skip the Poisson serving leg")
     ap.add_argument("--no-stress", action="store_true", help="skip the 4096x3000/512 stress rig")
+    ap.add_argument("--no-modes3", action="store_true", help="skip the three-output compute_disparities key")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
     if args.rig:

@@ -160,7 +160,7 @@ constexpr int kMedPairs = 2; // packed position pairs per thread
 constexpr int kMedPF = 3;
 __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, const Geom &g, uint16_t *__restrict__ med,
                                            int k, const unsigned *rowflags, unsigned epoch, unsigned *err,
-                                           unsigned wait_limit_us, uint16_t *msm) {
+                                           uint16_t *msm) {
     const int f = k >> 1;
     const int H = g.frows(f), W = g.fcols(f);
     const int N = W * H; // a multiple of 16 (W and H are multiples of 4)
@@ -190,7 +190,7 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
             if (n % 64 == 0) {
                 // one lane decides, so that `ready` stays the same in every lane
                 const bool expired =
-                    lane == 0 && (*(volatile unsigned *)err != kErrNone || global_ns() - t0 > 1000ull * wait_limit_us);
+                    lane == 0 && (*(volatile unsigned *)err != kErrNone || global_ns() - t0 > 1000ull * kDefaultWaitUs);
                 if (__any_sync(0xFFFFFFFFu, expired)) {
                     if (lane == 0) atomicCAS(err, kErrNone, kErrTimeout);
                     ready = H;
@@ -295,9 +295,9 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
 
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
                                                       uint16_t *__restrict__ med, int k0, const unsigned *rowflags,
-                                                      unsigned epoch, unsigned *err, unsigned wait_limit_us) {
+                                                      unsigned epoch, unsigned *err) {
     extern __shared__ __align__(16) uint16_t msm[];
-    median_map(wta, g, med, k0 + blockIdx.x, rowflags, epoch, err, wait_limit_us, msm);
+    median_map(wta, g, med, k0 + blockIdx.x, rowflags, epoch, err, msm);
 }
 
 // Both WTAs of every frame row and the eight medians in one launch: blocks 0..7 sweep the medians of maps
@@ -308,11 +308,10 @@ __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict
 // dispatch order completes.
 __global__ void __launch_bounds__(1024) wta_median_kernel(const uint64_t *__restrict__ census, Geom g,
                                                           uint16_t *__restrict__ wta, uint16_t *__restrict__ med,
-                                                          unsigned *rowflags, unsigned epoch, unsigned *err,
-                                                          unsigned wait_limit_us) {
+                                                          unsigned *rowflags, unsigned epoch, unsigned *err) {
     extern __shared__ __align__(16) uint64_t fsm[];
     if (blockIdx.x < 8) {
-        median_map(wta, g, med, blockIdx.x, rowflags, epoch, err, wait_limit_us, reinterpret_cast<uint16_t *>(fsm));
+        median_map(wta, g, med, blockIdx.x, rowflags, epoch, err, reinterpret_cast<uint16_t *>(fsm));
         return;
     }
     // row t of the merged sequence: A = rows of frames 1 and 3 (2 Wp), B = rows of frames 0 and 2 (2 Hp)
@@ -411,17 +410,17 @@ void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaS
 }
 
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf,
-                   const unsigned *rowflags, unsigned epoch, unsigned *err, unsigned wait_limit_us) {
+                   const unsigned *rowflags, unsigned epoch, unsigned *err) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     // one thread per kMedPairs position pairs of a chunk (W-1 positions), plus one for the odd ends
     int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
     threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
-    median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err, wait_limit_us);
+    median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err);
 }
 
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
-                       unsigned epoch, unsigned *err, cudaStream_t st, unsigned wait_limit_us) {
+                       unsigned epoch, unsigned *err, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
@@ -429,7 +428,7 @@ void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uin
     threads = threads < 256 ? 256 : threads > 1024 ? 1024 : threads;
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
-                                                                                       epoch, err, wait_limit_us);
+                                                                                       epoch, err);
 }
 
 void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16_t *outR, cudaStream_t st) {

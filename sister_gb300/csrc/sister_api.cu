@@ -62,6 +62,11 @@ struct sister_ctx {
     bool loaded = false;
     int w = 0, h = 0, dc = 0;
     DevBuf raw, views, frames, census, wta, med, masks, cost, sum0, sum1, bnd, progress, errflag, disp, outs;
+    // several modes in one call: per extra mode its own cost, sum and hand-off buffers, and the device descriptors
+    // (rigs, work items, item ticket) of one multi-job aggregation launch
+    DevBuf modevols, desc;
+    int desc_key[4] = {0, 0, 0, 0}; // w, h, dc, mode mask the descriptors were built for
+    SgmRig desc_rigs[3] = {};        // and the buffers they point to
     // pair WTA row flags: [4][max(Wp, Hp)] u32 holding the epoch (compute count) in which the row was written
     DevBuf rowflags;
     unsigned epoch = 0;
@@ -85,6 +90,7 @@ struct sister_ctx {
         ev_stage.push_back(stage);
     }
     int last_mode = -1;
+    const uint16_t *last_cost = nullptr, *last_sum0 = nullptr; // volumes of the last aggregated mode
     bool have_intermediates = false;
     Geom g{};
 
@@ -206,6 +212,98 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
     return SISTER_OK;
 }
 
+// Several modes of one rig (the reference's compute_disparities computes all three, hpp:77-89): each mode's masked
+// cost into its own volume, then ONE aggregation launch over the work items of every mode (items ordered by
+// band, so each follows the previous band of its mode and pass), then each mode's final WTA. One launch instead of
+// one per mode: the wavefront ramp and tail of each mode are filled by the other modes' bands.
+int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16_t *dev_out[3]) {
+    cudaStream_t st = c->stream;
+    int modes[3], nm = 0, mask = 0;
+    for (int m = 0; m < 3; m++)
+        if (dev_out[m]) {
+            modes[nm++] = m;
+            mask |= 1 << m;
+        }
+    const size_t vol = g.plane * g.dp * sizeof(uint16_t), bnd = sgm_bnd_bytes(g, plan);
+    const size_t prog = sgm_progress_bytes(std::max(plan.ngroups, 1));
+    const size_t per = 3 * vol + bnd + prog; // cost, sum0, sum1, hand-off records, progress counters
+    cudaError_t e = c->modevols.ensure((size_t)(nm - 1) * per);
+    if (e != cudaSuccess) return c->cuda_fail(e, "per-mode volumes");
+    SgmRig rg[3];
+    std::memset(rg, 0, sizeof rg);
+    for (int k = 0; k < nm; k++) {
+        SgmRig &a = rg[k];
+        if (k == 0) {
+            a.cost = c->cost.as<uint16_t>();
+            a.sum0 = c->sum0.as<uint16_t>();
+            a.sum1 = c->sum1.as<uint16_t>();
+            a.bnd = c->bnd.as<uint16_t>();
+            a.progress = c->progress.as<unsigned>();
+        } else {
+            char *b = c->modevols.as<char>() + (size_t)(k - 1) * per;
+            a.cost = reinterpret_cast<uint16_t *>(b);
+            a.sum0 = reinterpret_cast<uint16_t *>(b + vol);
+            a.sum1 = reinterpret_cast<uint16_t *>(b + 2 * vol);
+            a.bnd = reinterpret_cast<uint16_t *>(b + 3 * vol);
+            a.progress = reinterpret_cast<unsigned *>(b + 3 * vol + bnd);
+        }
+        a.W = g.Wp;
+        a.H = g.Hp;
+        a.D = g.dc;
+        a.nbands = plan.nbands;
+    }
+    const int nitems = 2 * plan.nbands * nm;
+    const size_t rig_bytes = 3 * sizeof(SgmRig), item_off = (rig_bytes + 255) & ~(size_t)255;
+    const size_t claim_off = (item_off + (size_t)nitems * 4 + 255) & ~(size_t)255;
+    e = c->desc.ensure(claim_off + progress_bytes(1));
+    if (e != cudaSuccess) return c->cuda_fail(e, "aggregation descriptors");
+    char *desc = c->desc.as<char>();
+    if (c->desc_key[0] != g.w || c->desc_key[1] != g.h || c->desc_key[2] != g.dc || c->desc_key[3] != mask ||
+        std::memcmp(c->desc_rigs, rg, (size_t)nm * sizeof(SgmRig)) != 0) {
+        std::vector<uint32_t> items;
+        items.reserve(nitems);
+        for (int band = 0; band < plan.nbands; band++)
+            for (int k = 0; k < nm; k++)
+                for (uint32_t pass = 0; pass < 2; pass++) items.push_back((uint32_t)k << 24 | (uint32_t)band << 1 | pass);
+        e = cudaMemcpyAsync(desc, rg, rig_bytes, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(desc + item_off, items.data(), items.size() * 4, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st); // the host vectors go out of scope
+        if (e != cudaSuccess) return c->cuda_fail(e, "aggregation descriptors");
+        c->desc_key[0] = g.w;
+        c->desc_key[1] = g.h;
+        c->desc_key[2] = g.dc;
+        c->desc_key[3] = mask;
+        std::memcpy(c->desc_rigs, rg, (size_t)nm * sizeof(SgmRig));
+    }
+    for (int k = 0; k < nm; k++) {
+        launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, modes[k], const_cast<uint16_t *>(rg[k].cost),
+                           st);
+        e = cudaMemsetAsync(rg[k].progress, 0, prog, st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "progress counters");
+    }
+    c->mark(SISTER_STAGE_COST);
+    e = cudaMemsetAsync(desc + claim_off, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess)
+        e = launch_sgm_multi(g.dp, plan.R, reinterpret_cast<const SgmRig *>(desc),
+                             reinterpret_cast<const uint32_t *>(desc + item_off), nitems,
+                             reinterpret_cast<unsigned *>(desc + claim_off), c->errflag.as<unsigned>(), c->device, st,
+                             c->wait_limit_us);
+    if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
+    c->mark(SISTER_STAGE_AGGREGATE);
+    for (int k = 0; k < nm; k++) {
+        e = launch_sgm_wta(g, rg[k].sum0, rg[k].sum1, dev_out[modes[k]],
+                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)modes[k] * g.plane : nullptr, st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
+    }
+    c->mark(SISTER_STAGE_WTA);
+    c->last_mode = modes[nm - 1];
+    c->last_cost = rg[nm - 1].cost;
+    c->last_sum0 = rg[nm - 1].sum0;
+    c->have_intermediates = true;
+    return SISTER_OK;
+}
+
 // The whole compute_disparities pipeline on the context stream; outputs (device) may be null.
 int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     if (!c->loaded) return c->fail(SISTER_ESTATE, "no views loaded");
@@ -231,7 +329,7 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     // profiling on, the pair WTA stage covers that launch and the median stage is empty.
     if (++c->epoch == 0) c->epoch = 1;
     launch_wta_median(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), c->med.as<uint16_t>(),
-                      c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st, c->wait_limit_us);
+                      c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st);
     c->mark(SISTER_STAGE_PAIR_WTA);
     c->mark(SISTER_STAGE_MEDIAN);
     launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
@@ -239,6 +337,8 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     e = cudaGetLastError();
     if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
     const SgmPlan &plan = plan_for(c, g);
+    const int nmodes = (dev_out[0] ? 1 : 0) + (dev_out[1] ? 1 : 0) + (dev_out[2] ? 1 : 0);
+    if (nmodes > 1) return run_modes_together(c, g, plan, dev_out);
     for (int mode = 0; mode < 3; mode++) {
         if (!dev_out[mode]) continue;
         launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
@@ -257,6 +357,8 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
         c->mark(SISTER_STAGE_WTA);
         c->last_mode = mode;
+        c->last_cost = a.cost;
+        c->last_sum0 = a.sum0;
     }
     c->have_intermediates = true;
     return SISTER_OK;
@@ -572,8 +674,8 @@ int sister_debug_fetch(sister_ctx *c, int what, int index, void *dst, size_t byt
     case SISTER_DBG_WTA: src = c->wta.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
     case SISTER_DBG_MEDIAN: src = c->med.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
     case SISTER_DBG_MASKS: src = c->masks.as<char>() + (size_t)index * plane; need = plane; break;
-    case SISTER_DBG_COST: src = c->cost.as<char>(); need = plane * g.dp * 2; break;
-    case SISTER_DBG_SUM0: src = c->sum0.as<char>(); need = plane * g.dp * 2; break;
+    case SISTER_DBG_COST: src = reinterpret_cast<const char *>(c->last_cost); need = plane * g.dp * 2; break;
+    case SISTER_DBG_SUM0: src = reinterpret_cast<const char *>(c->last_sum0); need = plane * g.dp * 2; break;
     case SISTER_DBG_DISP:
         if (!c->full_disp) return c->fail(SISTER_ESTATE, "the padded disparity map is kept only with SISTER_TUNE_FULL_DISP = 1");
         src = c->disp.as<char>() + (size_t)index * plane * 2;

@@ -432,7 +432,7 @@ int Engine::enqueue(Job *j, std::string *err) {
     if (ch == 3) launch_to_gray(src, (int)row, 3, w, h, views, st);
     launch_frames(views, g, reinterpret_cast<uint8_t *>(b + L.frames), st);
     launch_census(reinterpret_cast<uint8_t *>(b + L.frames), g, census, st);
-    launch_wta_median(census, g, wta, med, rowflags, 1u, errflag, st, wait_limit_us_);
+    launch_wta_median(census, g, wta, med, rowflags, 1u, errflag, st);
     launch_lrc_mask(med, g, masks, st);
     uint16_t *outs[3] = {r.multi, r.horiz, r.vert};
     int k = 0;

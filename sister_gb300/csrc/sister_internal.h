@@ -91,12 +91,12 @@ void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaS
 // same flags waits for the rows it reads, so it may be launched before the frame's pair WTA has finished.
 void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4,
                      unsigned *rowflags = nullptr, unsigned epoch = 0);
+// the medians' row-flag waits use the default limit (kDefaultWaitUs)
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4,
-                   const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr,
-                   unsigned wait_limit_us = kDefaultWaitUs);
+                   const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr);
 // pair WTA of every frame and the eight medians in one launch (medians follow the rows through rowflags)
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
-                       unsigned epoch, unsigned *err, cudaStream_t st, unsigned wait_limit_us = kDefaultWaitUs);
+                       unsigned epoch, unsigned *err, cudaStream_t st);
 // two-view doStereo tail: LR-checked left map (-10 where rejected) and the right map, from frame 0's medians
 void launch_stereo_lrc(const uint16_t *med, const Geom &g, int16_t *outL, uint16_t *outR, cudaStream_t st);
 void launch_lrc_mask(const uint16_t *med, const Geom &g, uint8_t *masks, cudaStream_t st, int f0 = 0, int nf = 4);
