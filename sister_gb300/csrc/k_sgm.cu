@@ -80,7 +80,8 @@ __host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
     L.nbar = 2 * L.nslot + in_batches(dp) + KI + 2 * R;
     size_t o = 0;
     L.bars = o;
-    o += (size_t)L.nbar * 8 + 8; // + the writer's count of records copied to global memory (u32)
+    o += (size_t)L.nbar * 8 + 16; // + the writer's count of records copied to global memory (u32) and the CTA's
+                                  // current work item (int)
     o = (o + 127) & ~(size_t)127;
     L.rings = o;
     o += (size_t)L.nslot * rec_u16(dp) * 2;
@@ -336,12 +337,12 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
     // Work items are drawn from a ticket in item order, so every item a CTA waits on (the previous band of its
     // pass) was drawn earlier by a CTA that is running or done: the launch completes however many of its CTAs
     // are resident, and needs no cooperative launch -- other kernels may share the GPU with it.
-    __shared__ int s_item;
+    volatile int *s_item = reinterpret_cast<volatile int *>(smem + L.bars + 8u * (uint32_t)L.nbar + 8u);
     bool first_band = true;
     for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(a.claim, 1u);
+        if (threadIdx.x == 0) *s_item = (int)atomicAdd(a.claim, 1u);
         __syncthreads();
-        const int item = s_item;
+        const int item = *s_item;
         if (item >= a.nitems) break;
         int band;
         SgmRig rg;
