@@ -21,53 +21,70 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // WTALeft_SSE / WTARight_SSE with uniqueness 1 (postprocess.cpp:74-315) on a pair's Hamming volume
 // (census.cpp:54-146), without materialising the volume. Both reduce to the lowest-index argmin of the
-// same keys key(a, b) = popc(Cc[a] ^ Cn[b]) << 16 | (a - b) over the band 0 <= a - b < D:
+// same keys over the band 0 <= d = a - b < D of a frame row:
 //   L(a) = min over b of key(a, b)   (d = a - b <= min(a, D-1))
 //   R(b) = min over a of key(a, b)   (k = a - b <= min(D-1, W-1-b))
-// so every cell is counted once. A warp owns 32 consecutive columns b (one per lane) and walks the
-// diagonals d = 0..D-1, four per step: lane l keeps R of its column in a register and carries the partial L
-// of row a = b0+l+d, which moves down the lanes as d grows; rows whose cells in this block are all seen are
-// merged into a shared array with atomicMin.
+// so every cell is counted once. Keys are 16 bits, popc(Cc[a] ^ Cn[b]) << 9 | d (popcount <= 64, d < 512): the
+// lowest key is the lowest cost and, among equal costs, the lowest d, which is the reference's tie rule. Two
+// cells share each 32-bit word, so every packed minimum and every shuffle serves two columns.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
-// One CTA per frame row; both census rows staged in shared memory.
-// Four diagonals per step: lane l meets cells (b0+l+d+i, b0+l) for i = 0..3. Before the step lane l carries
-// the partial L of row a = b0+l+d; that row gets cell i of lane l-i (i <= l). A shuffle of cell i from lane
-// (l-i) mod 32 hands lane l either a cell of its own row (i <= l) or, wrapping around, a cell of the row that
-// enters the warp at lane 28+l after the step (i > l: cells of lanes 29..31). After the step the rows of lanes
-// 0..3 have no later cell in this block: they are merged into shared memory and the partials move four lanes
-// down, lanes 28..31 taking the entering rows. dmax is a multiple of 4 (D is a multiple of 8, W - b0 of 4).
+// One CTA per frame row; both census rows are staged in shared memory, and the row's band is cut into work
+// units of 64 columns x 64 diagonals spread over the CTA's warps.
+// In a unit, lane l holds columns bA = b0+l (low halves) and bB = b0+32+l (high halves) and walks the diagonals
+// four per step: it meets cells (bA+d+i, bA) and (bB+d+i, bB) for i = 0..3. R of both columns stays in a register.
+// Before the step lane l carries the partial L of rows bA+d and bB+d; those rows get cell i of lane l-i (i <= l). A
+// shuffle of cell i from lane (l-i) mod 32 hands lane l either a cell of its own rows (i <= l) or, wrapping around,
+// a cell of the rows that enter the warp at lane 28+l after the step (i > l: cells of lanes 29..31). After the
+// step the rows of lanes 0..3 have no later cell in this unit: they are merged into shared memory and the
+// partials move four lanes down, lanes 28..31 taking the entering rows. Partials still held at the end of a unit
+// and the R of its columns are merged too (shared atomicMin). d0 and d1 are multiples of 4.
+constexpr unsigned FULLW = 0xFFFFFFFFu;
+constexpr int kWtaCols = 64, kWtaDiags = 64; // a work unit
+
 template <bool EDGE>
-__device__ __forceinline__ void wta_block(const uint64_t *cc, uint64_t cb, int b0, int lane, int W, int dmax,
-                                          uint32_t *lk, uint32_t &racc) {
-    uint32_t lacc = 0xFFFFFFFFu;
-    const int b = b0 + lane;
-    // OR masks: a shuffled cell i counts for this lane's row when i <= lane, else for the entering row
+__device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t cbA, uint64_t cbB, int b0, int lane, int W,
+                                         int d0, int d1, uint32_t *lk, uint32_t *rk) {
+    const int bA = b0 + lane, bB = bA + 32;
+    uint32_t lacc = FULLW, racc = FULLW;
+    // OR masks: a shuffled cell i counts for this lane's rows when i <= lane, else for the entering rows
     const uint32_t m1 = lane >= 1 ? 0u : ~0u, m2 = lane >= 2 ? 0u : ~0u, m3 = lane >= 3 ? 0u : ~0u;
-#pragma unroll 8 // 8.74 against 8.90 ms per 1920x1080/256 rig for 2
-    for (int d = 0; d < dmax; d += 4) {
-        const int a = b + d;
+#pragma unroll 4
+    for (int d = d0; d < d1; d += 4) {
         uint32_t k[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const uint64_t x = cc[EDGE ? min(a + i, W - 1) : a + i] ^ cb;
-            k[i] = ((uint32_t)__popcll(x) << 16) | (uint32_t)(d + i);
-            if (EDGE && a + i >= W) k[i] = 0xFFFFFFFFu;
+            const int aA = bA + d + i, aB = bB + d + i;
+            const uint64_t xA = cc[EDGE ? min(aA, W - 1) : aA] ^ cbA;
+            const uint64_t xB = cc[EDGE ? min(aB, W - 1) : aB] ^ cbB;
+            const uint32_t pk = (uint32_t)__popcll(xA) | ((uint32_t)__popcll(xB) << 16);
+            k[i] = (pk << 9) | ((uint32_t)(d + i) * 0x10001u);
+            if (EDGE) {
+                if (aA >= W) k[i] |= 0x0000FFFFu;
+                if (aB >= W) k[i] |= 0xFFFF0000u;
+            }
         }
-        racc = __vimin3_u32(racc, __vimin3_u32(k[0], k[1], k[2]), k[3]);
-        const uint32_t s1 = __shfl_sync(0xFFFFFFFFu, k[1], (lane + 31) & 31);
-        const uint32_t s2 = __shfl_sync(0xFFFFFFFFu, k[2], (lane + 30) & 31);
-        const uint32_t s3 = __shfl_sync(0xFFFFFFFFu, k[3], (lane + 29) & 31);
-        lacc = __vimin3_u32(__vimin3_u32(lacc, k[0], s1 | m1), s2 | m2, s3 | m3);
-        const uint32_t ent = __vimin3_u32(s1 | ~m1, s2 | ~m2, s3 | ~m3);
-        if (lane < 4) atomicMin(&lk[b0 + d + lane], lacc); // rows b0+d .. b0+d+3: complete for this block
-        lacc = __shfl_sync(0xFFFFFFFFu, lane < 4 ? ent : lacc, (lane + 4) & 31);
+        racc = __vimin3_u16x2(racc, __vimin3_u16x2(k[0], k[1], k[2]), k[3]);
+        const uint32_t s1 = __shfl_sync(FULLW, k[1], (lane + 31) & 31);
+        const uint32_t s2 = __shfl_sync(FULLW, k[2], (lane + 30) & 31);
+        const uint32_t s3 = __shfl_sync(FULLW, k[3], (lane + 29) & 31);
+        lacc = __vimin3_u16x2(__vimin3_u16x2(lacc, k[0], s1 | m1), s2 | m2, s3 | m3);
+        const uint32_t ent = __vimin3_u16x2(s1 | ~m1, s2 | ~m2, s3 | ~m3);
+        if (lane < 4) { // rows bA+d (< W: d < W - b0 - 3) and bB+d are complete for this unit
+            atomicMin(&lk[bA + d], lacc & 0xFFFFu);
+            if (!EDGE || bB + d < W) atomicMin(&lk[bB + d], lacc >> 16);
+        }
+        lacc = __shfl_sync(FULLW, lane < 4 ? ent : lacc, (lane + 4) & 31);
     }
-    // lane l now carries row a = b0 + l + dmax, which may still have cells in later diagonals of other blocks
-    if (b + dmax < W && lacc != 0xFFFFFFFFu) atomicMin(&lk[b + dmax], lacc);
+    // lane l now carries rows bA+d1 and bB+d1, which may have cells in other units
+    if (bA + d1 < W && (lacc & 0xFFFFu) != 0xFFFFu) atomicMin(&lk[bA + d1], lacc & 0xFFFFu);
+    if (bB + d1 < W && (lacc >> 16) != 0xFFFFu) atomicMin(&lk[bB + d1], lacc >> 16);
+    if (bA < W) atomicMin(&rk[bA], racc & 0xFFFFu);
+    if (bB < W) atomicMin(&rk[bB], racc >> 16);
 }
 
 // With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
 // i] = epoch (release), so that the frame's median can start on the first rows while later rows are computed.
+// Shared memory: both census rows (2 W words) and the L and R key arrays (2 W u32).
 __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census, const Geom &g,
                                              uint16_t *__restrict__ wta, int f, int i, unsigned *rowflags,
                                              unsigned epoch, uint64_t *srow) {
@@ -81,27 +98,33 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
         }
     } else {
         uint64_t *cc = srow, *cn = srow + W;
-        uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W);
+        uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W), *rk = lk + W;
         const uint64_t *gc = census + (size_t)(2 * f) * g.plane + (size_t)i * W;
         const uint64_t *gn = census + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
         for (int j = threadIdx.x; j < W; j += blockDim.x) {
             cc[j] = gc[j];
             cn[j] = gn[j];
-            lk[j] = 0xFFFFFFFFu;
+            lk[j] = FULLW;
+            rk[j] = FULLW;
         }
         __syncthreads();
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        for (int blk = warp; blk * 32 < W; blk += nw) {
-            const int b0 = 32 * blk, b = b0 + lane;
-            const uint64_t cb = cn[min(b, W - 1)];
-            const int dmax = min(D, W - b0);
-            uint32_t racc = 0xFFFFFFFFu;
-            if (b0 + 31 + dmax - 1 < W) wta_block<false>(cc, cb, b0, lane, W, dmax, lk, racc);
-            else wta_block<true>(cc, cb, b0, lane, W, dmax, lk, racc);
-            if (b < W) R[b] = (uint16_t)(racc & 0xFFFFu);
+        const int nblk = (W + kWtaCols - 1) / kWtaCols, nch = (D + kWtaDiags - 1) / kWtaDiags;
+        for (int u = warp; u < nblk * nch; u += nw) {
+            const int blk = u / nch, ch = u - blk * nch;
+            const int b0 = kWtaCols * blk;
+            const int dmax = min(D, W - b0); // a multiple of 4 (D of 8, W of 4, b0 of 64)
+            const int d0 = kWtaDiags * ch, d1 = min(d0 + kWtaDiags, dmax);
+            if (d0 >= d1) continue; // warp-uniform
+            const uint64_t cbA = cn[min(b0 + lane, W - 1)], cbB = cn[min(b0 + 32 + lane, W - 1)];
+            if (b0 + kWtaCols - 1 + d1 - 1 < W) wta_unit<false>(cc, cbA, cbB, b0, lane, W, d0, d1, lk, rk);
+            else wta_unit<true>(cc, cbA, cbB, b0, lane, W, d0, d1, lk, rk);
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < W; j += blockDim.x) L[j] = (uint16_t)(lk[j] & 0xFFFFu);
+        for (int j = threadIdx.x; j < W; j += blockDim.x) {
+            L[j] = (uint16_t)(lk[j] & 0x1FFu);
+            R[j] = (uint16_t)(rk[j] & 0x1FFu);
+        }
     }
     if (rowflags) {
         __syncthreads();
@@ -110,15 +133,6 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
             st_release_u32(rowflags + (size_t)f * max(g.Wp, g.Hp) + i, epoch);
         }
     }
-}
-
-__global__ void __launch_bounds__(256) pair_wta_kernel(const uint64_t *__restrict__ census, Geom g,
-                                                       uint16_t *__restrict__ wta, int f0, unsigned *rowflags,
-                                                       unsigned epoch) {
-    extern __shared__ uint64_t srow[];
-    const int f = f0 + blockIdx.y;
-    if ((int)blockIdx.x >= g.frows(f)) return;
-    pair_wta_row(census, g, wta, f, blockIdx.x, rowflags, epoch, srow);
 }
 
 // shared ring length for the median sweep: a power of two >= 2W
@@ -393,20 +407,12 @@ void init_mask_kernels() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncSetAttribute(pair_wta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncAttributes fa{};
     cudaFuncGetAttributes(&fa, median_kernel); // its mbarriers are static shared memory
     cudaFuncSetAttribute(median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
     cudaFuncGetAttributes(&fa, wta_median_kernel);
     cudaFuncSetAttribute(wta_median_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
     cudaGetLastError();
-}
-
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0, int nf,
-                     unsigned *rowflags, unsigned epoch) {
-    const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
-    pair_wta_kernel<<<dim3(mx, nf), 256, smem, st>>>(census, g, wta, f0, rowflags, epoch);
 }
 
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0, int nf,
@@ -422,7 +428,7 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
                        unsigned epoch, unsigned *err, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + (size_t)mx * sizeof(uint32_t);
+    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t);
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
     threads = threads < 256 ? 256 : threads > 1024 ? 1024 : threads;

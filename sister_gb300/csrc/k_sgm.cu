@@ -42,6 +42,7 @@
 // inside a pair whose sums are never read (the final minimum masks d >= dc).
 // Every wait is bounded: on expiry the device error flag is raised and the kernel finishes.
 #include "sister_internal.h"
+#include "tuned_gb300.h"
 
 #include <algorithm>
 #include <vector>
@@ -832,6 +833,13 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
     const void *fn = kernel_for(g.dpl);
     if (!fn) return SgmPlan{};
     const int rmax = sgm_rows_max(g.dp, device);
+    // on a 152-SM GB300, the band height the autotuner measured fastest for this geometry's class
+    if (!force_R && sms == 152)
+        for (const TunedRows &t : kTunedRows)
+            if (t.dp == g.dp && g.Hp >= t.hp_lo && g.Hp < t.hp_hi && t.rows >= 1 && t.rows <= rmax) {
+                force_R = t.rows;
+                break;
+            }
     const int lo = force_R ? std::max(1, std::min(rmax, force_R)) : 1;
     return plan_rows(g, sms, lo, force_R ? lo : rmax, [&](int R) {
         int k = 0;

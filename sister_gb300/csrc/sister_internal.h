@@ -89,8 +89,7 @@ void launch_census(const uint8_t *frames, const Geom &g, uint64_t *census, cudaS
 // the mask stages run on frames [f0, f0 + nf) (all four by default)
 // rowflags (4 x max(Wp, Hp) u32, or null): pair WTA publishes each frame row with `epoch`; a median given the
 // same flags waits for the rows it reads, so it may be launched before the frame's pair WTA has finished.
-void launch_pair_wta(const uint64_t *census, const Geom &g, uint16_t *wta, cudaStream_t st, int f0 = 0, int nf = 4,
-                     unsigned *rowflags = nullptr, unsigned epoch = 0);
+
 // the medians' row-flag waits use the default limit (kDefaultWaitUs)
 void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream_t st, int f0 = 0, int nf = 4,
                    const unsigned *rowflags = nullptr, unsigned epoch = 0, unsigned *err = nullptr);
