@@ -29,6 +29,10 @@ namespace {
 constexpr size_t kAlign = 256;
 constexpr int kMaxSlots = 16;
 constexpr size_t kKeepUnwaited = 4096; // finished tickets nobody waited for: the oldest beyond this are dropped
+// Rigs of at most this many padded cells (Wp*Hp*dp; 1920x1080 at 256 disparities is 0.99 G) run on high-priority
+// streams: when SMs free up, their pending blocks are dispatched before those of larger rigs, so a smaller
+// request admitted next to a large one is not held behind every block of the large one.
+constexpr double kHighPrioCells = 1.2e9;
 
 size_t al(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
@@ -117,6 +121,7 @@ int validate(const sister_rig &r, std::string *err) {
 } // namespace
 
 struct Engine::Job {
+    cudaStream_t st = nullptr; // its slot's stream: high priority for rigs up to kHighPrioCells padded cells
     Engine *eng = nullptr;
     uint64_t ticket = 0;
     sister_rig rig{};
@@ -173,9 +178,14 @@ int Engine::create(Engine **out, int device, size_t budget, const Limits &lim, s
         cudaMemPoolSetAttribute(e->pool_, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
     e->streams_.assign(kMaxSlots, nullptr);
+    e->streams_hi_.assign(kMaxSlots, nullptr);
     e->pinned_.assign(kMaxSlots, Pinned{});
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
     for (int s = 0; s < kMaxSlots && ce == cudaSuccess; s++) {
         ce = cudaStreamCreateWithFlags(&e->streams_[s], cudaStreamNonBlocking);
+        if (ce == cudaSuccess)
+            ce = cudaStreamCreateWithPriority(&e->streams_hi_[s], cudaStreamNonBlocking, prio_greatest);
         if (ce == cudaSuccess) ce = cudaHostAlloc(&e->pinned_[s].p, kAlign, cudaHostAllocDefault);
         e->pinned_[s].cap = kAlign;
     }
@@ -199,11 +209,12 @@ Engine::~Engine() {
     cv_work_.notify_all();
     if (worker_.joinable()) worker_.join();
     cudaSetDevice(device_);
-    for (cudaStream_t s : streams_)
-        if (s) {
-            cudaStreamSynchronize(s);
-            cudaStreamDestroy(s);
-        }
+    for (auto *v : {&streams_, &streams_hi_})
+        for (cudaStream_t s : *v)
+            if (s) {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
     for (Pinned &p : pinned_)
         if (p.p) cudaFreeHost(p.p);
     if (pool_) cudaMemPoolDestroy(pool_);
@@ -324,6 +335,7 @@ void Engine::run() {
             queue_.pop_front();
             j->slot = free_slots_.back();
             free_slots_.pop_back();
+            j->st = (double)j->g.plane * j->g.dp <= kHighPrioCells ? streams_hi_[j->slot] : streams_[j->slot];
             reserved_ += j->bytes;
             inflight_++;
             peak_inflight_ = std::max(peak_inflight_, inflight_);
@@ -378,7 +390,7 @@ void Engine::admit(Job *j) {
     }
     if (status != SISTER_OK) {
         // nothing of this rig remains queued on its stream once it is synchronised
-        cudaStream_t st = streams_[j->slot];
+        cudaStream_t st = j->st;
         cudaStreamSynchronize(st);
         if (j->mem) cudaFreeAsync(j->mem, st);
         cudaStreamSynchronize(st);
@@ -396,7 +408,7 @@ int Engine::enqueue(Job *j, std::string *err) {
     const Geom &g = j->g;
     const int w = r.width, h = r.height, ch = r.channels;
     const size_t img = (size_t)w * h;
-    cudaStream_t st = streams_[j->slot];
+    cudaStream_t st = j->st;
     const Layout L = layout(g, ch, j->nmodes, j->plan);
     cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void **>(&j->mem), L.total, pool_, st);
     if (e != cudaSuccess) {

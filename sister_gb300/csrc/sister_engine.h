@@ -60,7 +60,8 @@ class Engine {
     Limits lim_;
     unsigned wait_limit_us_ = kDefaultWaitUs;
     cudaMemPool_t pool_ = nullptr;
-    std::vector<cudaStream_t> streams_;
+    std::vector<cudaStream_t> streams_;    // per slot, default priority
+    std::vector<cudaStream_t> streams_hi_; // per slot, the device's highest priority (smaller rigs)
     std::vector<int> free_slots_;
     struct Pinned {
         void *p = nullptr;
