@@ -100,6 +100,11 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     const int i = i0 + w;
     if (i >= g.Hp) return;
     const int D = g.dc;
+    // window row of each frame, indexed by the column b - d: frames 0 and 2 read tile row w's staged row, frames 1
+    // and 3 the staged row of tile column jj (added per pixel)
+    const uint64_t *wbase[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) wbase[f] = win + (size_t)(f * kCostTile + ((f & 1) ? 0 : w)) * nwin - cost_win0(g, f, i0, j0);
     for (int jj = 0; jj < kCostTile; jj++) {
         const int j = j0 + jj;
         if (j >= g.Wp) break;
@@ -119,24 +124,37 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
                 continue;
             }
             const uint64_t cc = ctr[f][t];
-            const uint64_t *wr = win + (size_t)(f * kCostTile + ((f & 1) ? jj : w)) * nwin + (fb - cost_win0(g, f, i0, j0));
+            const uint64_t *wr = wbase[f] + ((f & 1) ? jj * nwin : 0) + fb;
             if (fb >= g.dp - 1) { // every d of the stride has its word (d >= dc reads one that is never used)
 #pragma unroll
                 for (int k = 0; k < DPL; k++) acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
             } else {
+                // d = lane + 32k: every lane has d <= b below k = b / 32 and none above it (warp-uniform), so only
+                // that one k tests per lane; d > b costs 255 (census.cpp:74-78)
+                const int kb = fb >> 5;
 #pragma unroll
                 for (int k = 0; k < DPL; k++) {
-                    const int d = lane + 32 * k;
-                    const uint64_t v = (d <= fb && d < D) ? wr[-d] : cc;
-                    acc[k] += d > fb ? 255u : (uint32_t)__popcll(cc ^ v);
+                    if (k < kb) {
+                        acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
+                    } else if (k == kb) {
+                        const int d = lane + 32 * k;
+                        acc[k] += d <= fb ? (uint32_t)__popcll(cc ^ wr[-d]) : 255u;
+                    } else {
+                        acc[k] += 255u;
+                    }
                 }
             }
         }
         uint16_t *out = cost + p * g.dp;
+        if (D == g.dp) { // every d of the stride is real
 #pragma unroll
-        for (int k = 0; k < DPL; k++) {
-            const int d = lane + 32 * k;
-            out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
+            for (int k = 0; k < DPL; k++) out[lane + 32 * k] = (uint16_t)acc[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < DPL; k++) {
+                const int d = lane + 32 * k;
+                out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
+            }
         }
     }
 }

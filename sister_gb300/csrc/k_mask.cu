@@ -25,61 +25,75 @@ __device__ __forceinline__ unsigned long long global_ns() {
 //   L(a) = min over b of key(a, b)   (d = a - b <= min(a, D-1))
 //   R(b) = min over a of key(a, b)   (k = a - b <= min(D-1, W-1-b))
 // so every cell is counted once. Keys are 16 bits, popc(Cc[a] ^ Cn[b]) << 9 | d (popcount <= 64, d < 512): the
-// lowest key is the lowest cost and, among equal costs, the lowest d, which is the reference's tie rule. Two
-// cells share each 32-bit word, so every packed minimum and every shuffle serves two columns.
+// lowest key is the lowest cost and, among equal costs, the lowest d, which is the reference's tie rule. Two keys
+// share each 32-bit word, so every packed minimum and every shuffle serves two cells.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
 // One CTA per frame row; both census rows are staged in shared memory, and the row's band is cut into work
 // units of 64 columns x 64 diagonals spread over the CTA's warps.
-// In a unit, lane l holds columns bA = b0+l (low halves) and bB = b0+32+l (high halves) and walks the diagonals
-// four per step: it meets cells (bA+d+i, bA) and (bB+d+i, bB) for i = 0..3. R of both columns stays in a register.
-// Before the step lane l carries the partial L of rows bA+d and bB+d; those rows get cell i of lane l-i (i <= l). A
-// shuffle of cell i from lane (l-i) mod 32 hands lane l either a cell of its own rows (i <= l) or, wrapping around,
-// a cell of the rows that enter the warp at lane 28+l after the step (i > l: cells of lanes 29..31). After the
-// step the rows of lanes 0..3 have no later cell in this unit: they are merged into shared memory and the
-// partials move four lanes down, lanes 28..31 taking the entering rows. Partials still held at the end of a unit
-// and the R of its columns are merged too (shared atomicMin). d0 and d1 are multiples of 4.
+// In a unit, lane l holds the adjacent columns cA = b0+2l and cB = cA+1 and walks the diagonals four per step.
+// At step d it meets cells A_i = (cA+d+i, cA) and B_i = (cB+d+i, cB), i = 0..3: eight cells from the five words
+// Cc[cA+d .. cA+d+4] (cA+d is even, so two 16-byte loads and one 8-byte load). R of both columns stays in a
+// register. Lane l carries the partial L of the row pair (cA+d, cA+d+1). That pair's cells this step are A0, and
+// A1 and B0, of lane l; A2 and B1, A3 and B2 of lane l-1; and B3 of lane l-2: lane l sends U = (min(A2, B1),
+// min(A3, B2)) to lane l+1 and V = (B3, -) to lane l+2. Lanes 0 and 1 receive, wrapping around, the cells of the
+// pairs that enter the warp after the step. After the step the pairs of lanes 0 and 1 (rows b0+d .. b0+d+3) have
+// no later cell in this unit: they are merged into shared memory, and the partials move two lanes down, lanes 30
+// and 31 taking the entering pairs. Partials still held at the end of a unit and the R of its columns are merged
+// too (shared atomicMin). d0 and d1 are multiples of 4.
 constexpr unsigned FULLW = 0xFFFFFFFFu;
 constexpr int kWtaCols = 64, kWtaDiags = 64; // a work unit
 
+__device__ __forceinline__ uint32_t keypair(uint32_t pa, uint32_t pb, uint32_t dd) {
+    return (pa | (pb << 16)) * 512u + dd; // (popc_a << 9 | d, popc_b << 9 | d): the halves never overlap
+}
+
 template <bool EDGE>
-__device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t cbA, uint64_t cbB, int b0, int lane, int W,
+__device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64_t wB, int b0, int lane, int W,
                                          int d0, int d1, uint32_t *lk, uint32_t *rk) {
-    const int bA = b0 + lane, bB = bA + 32;
+    const int cA = b0 + 2 * lane, cB = cA + 1;
     uint32_t lacc = FULLW, racc = FULLW;
-    // OR masks: a shuffled cell i counts for this lane's rows when i <= lane, else for the entering rows
-    const uint32_t m1 = lane >= 1 ? 0u : ~0u, m2 = lane >= 2 ? 0u : ~0u, m3 = lane >= 3 ? 0u : ~0u;
+    // OR masks: a received U (V) counts for this lane's pair when lane >= 1 (2), else for an entering pair
+    const uint32_t mU = lane >= 1 ? 0u : ~0u, mV = lane >= 2 ? 0u : ~0u;
 #pragma unroll 4
     for (int d = d0; d < d1; d += 4) {
-        uint32_t k[4];
+        uint64_t c[5];
+        if (EDGE) {
+#pragma unroll
+            for (int t = 0; t < 5; t++) c[t] = cc[min(cA + d + t, W - 1)];
+        } else {
+            const ulonglong2 p01 = *reinterpret_cast<const ulonglong2 *>(cc + cA + d);
+            const ulonglong2 p23 = *reinterpret_cast<const ulonglong2 *>(cc + cA + d + 2);
+            c[0] = p01.x; c[1] = p01.y; c[2] = p23.x; c[3] = p23.y;
+            c[4] = cc[cA + d + 4];
+        }
+        uint32_t kab[4]; // (A_i, B_i)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int aA = bA + d + i, aB = bB + d + i;
-            const uint64_t xA = cc[EDGE ? min(aA, W - 1) : aA] ^ cbA;
-            const uint64_t xB = cc[EDGE ? min(aB, W - 1) : aB] ^ cbB;
-            const uint32_t pk = (uint32_t)__popcll(xA) | ((uint32_t)__popcll(xB) << 16);
-            k[i] = (pk << 9) | ((uint32_t)(d + i) * 0x10001u);
+            kab[i] = keypair((uint32_t)__popcll(c[i] ^ wA), (uint32_t)__popcll(c[i + 1] ^ wB), (uint32_t)(d + i) * 0x10001u);
             if (EDGE) {
-                if (aA >= W) k[i] |= 0x0000FFFFu;
-                if (aB >= W) k[i] |= 0xFFFF0000u;
+                if (cA + d + i >= W) kab[i] |= 0x0000FFFFu;
+                if (cB + d + i >= W) kab[i] |= 0xFFFF0000u;
             }
         }
-        racc = __vimin3_u16x2(racc, __vimin3_u16x2(k[0], k[1], k[2]), k[3]);
-        const uint32_t s1 = __shfl_sync(FULLW, k[1], (lane + 31) & 31);
-        const uint32_t s2 = __shfl_sync(FULLW, k[2], (lane + 30) & 31);
-        const uint32_t s3 = __shfl_sync(FULLW, k[3], (lane + 29) & 31);
-        lacc = __vimin3_u16x2(__vimin3_u16x2(lacc, k[0], s1 | m1), s2 | m2, s3 | m3);
-        const uint32_t ent = __vimin3_u16x2(s1 | ~m1, s2 | ~m2, s3 | ~m3);
-        if (lane < 4) { // rows bA+d (< W: d < W - b0 - 3) and bB+d are complete for this unit
-            atomicMin(&lk[bA + d], lacc & 0xFFFFu);
-            if (!EDGE || bB + d < W) atomicMin(&lk[bB + d], lacc >> 16);
+        racc = __vimin3_u16x2(__vimin3_u16x2(racc, kab[0], kab[1]), kab[2], kab[3]);
+        const uint32_t own = __vminu2(__byte_perm(kab[0], kab[1], 0x5410), kab[0] | 0x0000FFFFu); // (A0, min(A1, B0))
+        const uint32_t u = __vminu2(__byte_perm(kab[2], kab[3], 0x5410), __byte_perm(kab[1], kab[2], 0x7632));
+        const uint32_t v = __byte_perm(kab[3], 0xFFFFFFFFu, 0x7632); // (B3, -)
+        const uint32_t ur = __shfl_sync(FULLW, u, (lane + 31) & 31);
+        const uint32_t vr = __shfl_sync(FULLW, v, (lane + 30) & 31);
+        lacc = __vminu2(__vimin3_u16x2(lacc, own, ur | mU), vr | mV);
+        const uint32_t ent = __vminu2(ur | ~mU, vr | ~mV);
+        if (lane < 2) { // rows cA+d and cA+d+1 (< W: the unit's rows stay below b0 + dmax) are complete here
+            atomicMin(&lk[cA + d], lacc & 0xFFFFu);
+            atomicMin(&lk[cA + d + 1], lacc >> 16);
         }
-        lacc = __shfl_sync(FULLW, lane < 4 ? ent : lacc, (lane + 4) & 31);
+        lacc = __shfl_sync(FULLW, lane < 2 ? ent : lacc, (lane + 2) & 31);
     }
-    // lane l now carries rows bA+d1 and bB+d1, which may have cells in other units
-    if (bA + d1 < W && (lacc & 0xFFFFu) != 0xFFFFu) atomicMin(&lk[bA + d1], lacc & 0xFFFFu);
-    if (bB + d1 < W && (lacc >> 16) != 0xFFFFu) atomicMin(&lk[bB + d1], lacc >> 16);
-    if (bA < W) atomicMin(&rk[bA], racc & 0xFFFFu);
-    if (bB < W) atomicMin(&rk[bB], racc >> 16);
+    // lane l now carries rows cA+d1 and cA+d1+1, which may have cells in other units
+    if (cA + d1 < W && (lacc & 0xFFFFu) != 0xFFFFu) atomicMin(&lk[cA + d1], lacc & 0xFFFFu);
+    if (cA + d1 + 1 < W && (lacc >> 16) != 0xFFFFu) atomicMin(&lk[cA + d1 + 1], lacc >> 16);
+    if (cA < W) atomicMin(&rk[cA], racc & 0xFFFFu);
+    if (cB < W) atomicMin(&rk[cB], racc >> 16);
 }
 
 // With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
@@ -116,9 +130,10 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
             const int dmax = min(D, W - b0); // a multiple of 4 (D of 8, W of 4, b0 of 64)
             const int d0 = kWtaDiags * ch, d1 = min(d0 + kWtaDiags, dmax);
             if (d0 >= d1) continue; // warp-uniform
-            const uint64_t cbA = cn[min(b0 + lane, W - 1)], cbB = cn[min(b0 + 32 + lane, W - 1)];
-            if (b0 + kWtaCols - 1 + d1 - 1 < W) wta_unit<false>(cc, cbA, cbB, b0, lane, W, d0, d1, lk, rk);
-            else wta_unit<true>(cc, cbA, cbB, b0, lane, W, d0, d1, lk, rk);
+            const uint64_t wA = cn[min(b0 + 2 * lane, W - 1)], wB = cn[min(b0 + 2 * lane + 1, W - 1)];
+            // the unit reads words up to cA + d1 (lane 31: b0 + 62 + d1)
+            if (b0 + kWtaCols - 2 + d1 < W) wta_unit<false>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk);
+            else wta_unit<true>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk);
         }
         __syncthreads();
         for (int j = threadIdx.x; j < W; j += blockDim.x) {
