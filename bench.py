@@ -350,6 +350,46 @@ def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 200
     return out
 
 
+def c1_leg(local):
+    """C1: the 640x480 rig at max disparity 192 (synth.rig_c1), plain path, views resident in HBM, L2 flushed
+    between computes; bit-exact check of the output against the reference's fixture."""
+    import numpy as np
+    import torch
+    import sister_gb300 as sg
+    from sister_gb300 import synth
+
+    (views, _), dc = synth.rig_c1(1)
+    h, w = views[0].shape
+    dev = [torch.from_numpy(v).cuda() for v in views]
+    out = torch.empty((h, w), dtype=torch.int16, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ctx = sg.Context(local)
+    st = torch.cuda.Stream()
+    ctx.set_stream(st.cuda_stream)
+    ctx.load_views_device([t.data_ptr() for t in dev], w, h, w, 1)
+    ctx.set_max_disparity(dc)
+    ctx.compute_device(out.data_ptr())
+    ctx.synchronize()
+    got = out.cpu().numpy().view(np.uint16)
+    try:
+        z = np.load(os.path.join(ROOT, "tests", "golden", "c1_640x480_dc192.npz"))
+        exact = hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest() == str(z["multi_sha"])
+    except Exception:
+        exact = None
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+    for a, b in ev:
+        with torch.cuda.stream(st):
+            flush.zero_()
+        a.record(st)
+        ctx.compute_device(out.data_ptr())
+        b.record(st)
+    ctx.synchronize()
+    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    ctx.close()
+    return {"workload": "640x480 u8, maxdisp 192, mode 0 (8-12 tiles, disparity 20-180)", "value": w * h * dc / 1e9 / (ms / 1e3),
+            "unit": UNIT, "ms_per_rig": ms, "bit_exact_vs_reference_golden": exact}
+
+
 def stress_leg(local):
     """C5: the 4096x3000 rig at max disparity 512 (synth.rig_c5), plain path, views resident in HBM."""
     import torch
@@ -531,6 +571,8 @@ def run_gb300(args):
             line["served"] = served_leg(local)
         if world == 1 and not args.no_stress:
             line["stress"] = stress_leg(local)
+        if world == 1 and not args.no_c1:
+            line["c1"] = c1_leg(local)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_c2(views, dc)
         print(json.dumps(line), flush=True)
@@ -604,6 +646,7 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the Poisson serving leg")
     ap.add_argument("--no-stress", action="store_true", help="skip the 4096x3000/512 stress rig")
     ap.add_argument("--no-modes3", action="store_true", help="skip the three-output compute_disparities key")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 640x480/192 key")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
     args = ap.parse_args()
     if args.rig:

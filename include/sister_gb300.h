@@ -117,7 +117,6 @@ enum {
     SISTER_STAGE_CENSUS = 2,   /* 9x7 census of the eight frame images */
     SISTER_STAGE_PAIR_WTA = 3, /* per-pair WTA-left/right from census words and, in the same launch, the
                                   row-recursive 3x3 medians that follow the WTA rows */
-    SISTER_STAGE_MEDIAN = 4,   /* kept for compatibility: the medians run inside the pair WTA stage (0 ms) */
     SISTER_STAGE_MASKS = 5,    /* LR check and confidence masks */
     SISTER_STAGE_COST = 6,     /* masked multiview cost volume (once per computed mode) */
     SISTER_STAGE_AGGREGATE = 7, /* 8-path aggregation, both passes concurrently (once per computed mode) */

@@ -25,7 +25,7 @@ SISTER_EINVAL, SISTER_ENOMEM, SISTER_EBUDGET, SISTER_EDEVICE, SISTER_ETIMEOUT, S
 SISTER_EBUSY, SISTER_EPENDING = -7, -8
 _ERRNAMES = {-1: "EINVAL", -2: "ENOMEM", -3: "EBUDGET", -4: "EDEVICE", -5: "ETIMEOUT", -6: "ESTATE"}
 
-STAGES = {1: "frames", 2: "census", 3: "pair_wta", 4: "median", 5: "masks", 6: "cost", 7: "aggregate", 8: "wta"}
+STAGES = {1: "frames", 2: "census", 3: "pair_wta", 5: "masks", 6: "cost", 7: "aggregate", 8: "wta"}
 TUNE_SGM_ROWS, TUNE_SGM_CLUSTER, TUNE_SGM_GROUPS, TUNE_SGM_CLUSTERS, TUNE_FULL_DISP, TUNE_WAIT_LIMIT_US = 1, 2, 3, 4, 5, 6
 DBG_FRAMES, DBG_CENSUS, DBG_WTA, DBG_MEDIAN, DBG_MASKS, DBG_COST, DBG_SUM0, DBG_DISP, DBG_DP = range(1, 10)
 

@@ -13,16 +13,15 @@ namespace {
 // The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
 // (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
 //
-// A CTA computes an 8x8 tile of padded pixels. The neighbour census words the tile needs are staged in shared
-// memory first, one window of dp + 10 words per frame row: frames 0 and 2 read the tile's 8 image rows, frames 1
-// and 3 (transposed) read one frame row per tile column, so each word is fetched from L2/HBM once per tile instead
-// of once per pixel (the transposed frames' rows are columns of the padded image); each pixel's centre words and
-// frame states (masked, constant row, or its column b) are staged too. Then warp w computes the 8 pixels of tile
-// row w, one at a time, lanes over d (lane l holds d = l + 32k, k < DPL), from shared memory only.
-// Frames whose column b >= dp-1 (most of them) skip the per-lane d > b test. Measured on 1920x1080/256: 1.40 ms
-// (1.65 without that shortcut) against 1.81 for one warp per pixel gathering from L1/L2. Summing the four
-// frames' XOR words with carry-save adders before counting (5 popcounts instead of 8 per d) was slower in every
-// form tried (2.2-3.5 ms): the popcount pipe is not the limit, the integer issue is.
+// A CTA computes an 8x8 tile of padded pixels. The transposed frames 1 and 3 read one frame row per tile column
+// (a column of the padded image), so their neighbour census windows (dp + 10 words per tile column) are staged in
+// shared memory first and each word is fetched from L2/HBM once per tile instead of once per pixel; frames 0 and 2
+// read one contiguous stretch of their census row per tile row, which consecutive pixels share through L1. Each
+// pixel's centre words and frame states (masked, constant row, or its column b) are staged too. Then warp w
+// computes the 8 pixels of tile row w, one at a time, lanes over d (lane l holds d = l + 32k, k < DPL). Frames whose
+// column b >= dp-1 (most of them) need no per-lane d > b test; nearer the left edge the test is one warp-uniform
+// branch per k. Summing the four frames' XOR words with carry-save adders before counting (5 popcounts instead
+// of 8 per d) was slower in every form tried (2.2-3.5 ms against 1.40): the popcount pipe is not the limit.
 constexpr int kCostTile = 8;
 constexpr int kNoCost = -3, kRow255 = -2, kRow0 = -1; // per-pixel frame states besides b >= 0
 __host__ __device__ inline int cost_win(int dp) { return dp + 10; } // words per staged frame row (even)
@@ -46,7 +45,7 @@ template <int DPL>
 __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__restrict__ census,
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
                                                           uint16_t *__restrict__ cost) {
-    extern __shared__ __align__(16) uint64_t win[]; // [frame][tile row][cost_win(dp)]
+    extern __shared__ __align__(16) uint64_t win[]; // [frame 1, 3][tile column][cost_win(dp)]
     // per frame and tile pixel: the centre census word, or kNoCost when the pixel's frame is unused (out of the
     // mode or masked) and kRow255 / kRow0 when its frame row is constant
     __shared__ uint64_t ctr[4][kCostTile * kCostTile];
@@ -75,14 +74,14 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
         fbs[f][t] = fb;
         ctr[f][t] = c;
     }
-    // ---- stage the windows: warp w copies staged rows w, w+8, w+16, w+24 (frame q / 8, tile row q % 8) with
-    // 16-byte asynchronous copies (windows start on even columns, frame rows on 16-byte boundaries); columns
-    // outside the frame row are never read and stay unwritten
-    for (int q = w; q < 4 * kCostTile; q += 8) {
-        const int f = q / kCostTile, r = q % kCostTile;
+    // ---- stage the transposed frames' windows: warp w copies staged rows w and w+8 (frame 1 then 3, tile column
+    // q % 8: frame row Wp-1-(j0+r)) with 16-byte asynchronous copies (windows start on even columns, frame rows on
+    // 16-byte boundaries); columns outside the frame row are never read and stay unwritten. Frames 0 and 2 need one
+    // contiguous stretch of their census row per tile row, read through L1 by the warps themselves.
+    for (int q = w; q < 2 * kCostTile; q += 8) {
+        const int f = q < kCostTile ? 1 : 3, r = q % kCostTile;
         if (!cost_in_mode(mode, f)) continue;
-        // frame row of tile row r: image row i0+r (frames 0, 2) or Wp-1-(j0+r) (frames 1, 3)
-        const int fa = (f & 1) ? g.Wp - 1 - (j0 + r) : i0 + r;
+        const int fa = g.Wp - 1 - (j0 + r);
         if (fa < 0 || fa >= g.frows(f)) continue;
         const int c0 = cost_win0(g, f, i0, j0), fw = g.fcols(f);
         const uint64_t *src = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa * fw;
@@ -100,11 +99,11 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     const int i = i0 + w;
     if (i >= g.Hp) return;
     const int D = g.dc;
-    // window row of each frame, indexed by the column b - d: frames 0 and 2 read tile row w's staged row, frames 1
-    // and 3 the staged row of tile column jj (added per pixel)
-    const uint64_t *wbase[4];
-#pragma unroll
-    for (int f = 0; f < 4; f++) wbase[f] = win + (size_t)(f * kCostTile + ((f & 1) ? 0 : w)) * nwin - cost_win0(g, f, i0, j0);
+    // neighbour census row of each frame, indexed by the column b - d: frames 0 and 2 the global row i, frames 1 and
+    // 3 the staged window of tile column jj
+    const uint64_t *grow0 = census + (size_t)1 * g.plane + (size_t)i * g.Wp; // frame 0 (fa = i)
+    const uint64_t *grow2 = census + (size_t)5 * g.plane + (size_t)i * g.Wp; // frame 2 (fa = i)
+    const int sw1 = -cost_win0(g, 1, i0, j0), sw3 = kCostTile * nwin - cost_win0(g, 3, i0, j0);
     for (int jj = 0; jj < kCostTile; jj++) {
         const int j = j0 + jj;
         if (j >= g.Wp) break;
@@ -124,7 +123,9 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
                 continue;
             }
             const uint64_t cc = ctr[f][t];
-            const uint64_t *wr = wbase[f] + ((f & 1) ? jj * nwin : 0) + fb;
+            const uint64_t *wr = (f == 0) ? grow0 + fb
+                                 : (f == 2) ? grow2 + fb
+                                 : win + (jj * nwin + (f == 1 ? sw1 : sw3) + fb);
             if (fb >= g.dp - 1) { // every d of the stride has its word (d >= dc reads one that is never used)
 #pragma unroll
                 for (int k = 0; k < DPL; k++) acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
@@ -137,8 +138,9 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
                     if (k < kb) {
                         acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
                     } else if (k == kb) {
-                        const int d = lane + 32 * k;
-                        acc[k] += d <= fb ? (uint32_t)__popcll(cc ^ wr[-d]) : 255u;
+                        const int d = lane + 32 * k; // the load stays inside the row: column b - min(d, b) >= 0
+                        const uint32_t h = (uint32_t)__popcll(cc ^ wr[-min(d, fb)]);
+                        acc[k] += d <= fb ? h : 255u;
                     } else {
                         acc[k] += 255u;
                     }
@@ -223,7 +225,7 @@ void launch_cost_dpl(const uint64_t *census, const uint8_t *masks, const Geom &g
         return;
     }
     dim3 grid((g.Wp + kCostTile - 1) / kCostTile, (g.Hp + kCostTile - 1) / kCostTile);
-    const size_t smem = (size_t)4 * kCostTile * cost_win(g.dp) * sizeof(uint64_t);
+    const size_t smem = (size_t)2 * kCostTile * cost_win(g.dp) * sizeof(uint64_t);
     masked_cost_kernel<DPL><<<grid, 256, smem, st>>>(census, masks, g, mode, cost);
 }
 

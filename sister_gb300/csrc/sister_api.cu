@@ -326,12 +326,11 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     c->mark(SISTER_STAGE_CENSUS);
     // Pair WTA of the four frames and the eight medians in one launch: the median blocks come first and follow
     // the WTA rows as they are published (each row with this compute's epoch); the masks follow. With
-    // profiling on, the pair WTA stage covers that launch and the median stage is empty.
+    // profiling on, the pair WTA stage covers that launch.
     if (++c->epoch == 0) c->epoch = 1;
     launch_wta_median(c->census.as<uint64_t>(), g, c->wta.as<uint16_t>(), c->med.as<uint16_t>(),
                       c->rowflags.as<unsigned>(), c->epoch, c->errflag.as<unsigned>(), st);
     c->mark(SISTER_STAGE_PAIR_WTA);
-    c->mark(SISTER_STAGE_MEDIAN);
     launch_lrc_mask(c->med.as<uint16_t>(), g, c->masks.as<uint8_t>(), st);
     c->mark(SISTER_STAGE_MASKS);
     e = cudaGetLastError();
