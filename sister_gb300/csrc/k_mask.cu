@@ -445,8 +445,12 @@ void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uin
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t);
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
+    // One block size for both kinds of block. The pair WTA rows run best at two blocks per SM (512 threads at its
+    // 61 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM); a median
+    // block needs one thread per kMedPairs position pairs of a chunk to sweep a chunk in one pass, and 512 threads
+    // take the longest chunks of frames up to 4096 columns in at most two passes, which their shorter chains absorb.
     int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
-    threads = threads < 256 ? 256 : threads > 1024 ? 1024 : threads;
+    threads = threads < 256 ? 256 : mx <= 4096 ? (threads > 512 ? 512 : threads) : (threads > 1024 ? 1024 : threads);
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
                                                                                        epoch, err);
