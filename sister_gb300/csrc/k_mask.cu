@@ -43,8 +43,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
 constexpr unsigned FULLW = 0xFFFFFFFFu;
 constexpr int kWtaCols = 64, kWtaDiags = 64; // a work unit
 
-__device__ __forceinline__ uint32_t keypair(uint32_t pa, uint32_t pb, uint32_t dd) {
-    return (pa | (pb << 16)) * 512u + dd; // (popc_a << 9 | d, popc_b << 9 | d): the halves never overlap
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+// (popc(xa) << 9 | d, popc(xb) << 9 | d) from the two 64-bit XOR words: four multiply-adds of the halves' popcounts
+// (the halves never overlap: popcounts <= 64, d < 512), which keep the key off the integer ALU pipe
+__device__ __forceinline__ uint32_t keypair(uint64_t xa, uint64_t xb, uint32_t dd) {
+    const uint32_t t1 = mad_u32((uint32_t)__popc((uint32_t)(xb >> 32)), 65536u, (uint32_t)__popc((uint32_t)(xa >> 32)));
+    const uint32_t t2 = mad_u32((uint32_t)__popc((uint32_t)xb), 65536u, (uint32_t)__popc((uint32_t)xa));
+    return mad_u32(t1, 512u, mad_u32(t2, 512u, dd));
 }
 
 template <bool EDGE>
@@ -69,7 +78,7 @@ __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64
         uint32_t kab[4]; // (A_i, B_i)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            kab[i] = keypair((uint32_t)__popcll(c[i] ^ wA), (uint32_t)__popcll(c[i + 1] ^ wB), (uint32_t)(d + i) * 0x10001u);
+            kab[i] = keypair(c[i] ^ wA, c[i + 1] ^ wB, (uint32_t)(d + i) * 0x10001u);
             if (EDGE) {
                 if (cA + d + i >= W) kab[i] |= 0x0000FFFFu;
                 if (cB + d + i >= W) kab[i] |= 0xFFFF0000u;
