@@ -158,19 +158,19 @@ typedef struct sister_rig {
     uint16_t *multi, *horiz, *vert; /* host outputs, width*height u16 each (disparity*255); NULL skips a mode */
 } sister_rig;
 typedef struct sister_batch sister_batch;
-/* budget_bytes: device memory the rigs in flight may hold together (0: three quarters of the device's free
- * memory), drawn from a pool owned by the batch. */
+/* budget_bytes: device memory the engine may hold, allocated here as one arena (0: three quarters of the
+ * device's free memory). */
 SISTER_API int sister_batch_create(sister_batch **out, int device, size_t budget_bytes);
 SISTER_API void sister_batch_destroy(sister_batch *batch);
 SISTER_API const char *sister_batch_last_error(sister_batch *batch);
-/* Computes every rig and returns when all outputs are written. Rigs are admitted continuously: each starts as
- * soon as a stream slot is free and its device memory fits the budget beside the rigs still running, and runs
- * the whole pipeline on its own stream, overlapping the others. A bad rig, or one that alone exceeds the budget,
- * fails the call (SISTER_EINVAL / SISTER_EBUDGET) before anything runs. Pinned (page-locked) host views and
- * outputs are used in place; pageable ones go through pinned staging. */
+/* Computes every rig and returns when all outputs are written. Rigs run in waves whose device memory fits the
+ * budget; within a wave the stages before the aggregation run per rig on several streams, and one persistent
+ * aggregation launch per disparity-stride class covers all of the wave's rigs and modes (work items ordered by
+ * band, so one rig's wavefront ramp is filled with the others' bands). A bad rig, or one that alone exceeds the
+ * budget, fails the call (SISTER_EINVAL / SISTER_EBUDGET) before anything runs. */
 SISTER_API int sister_batch_run(sister_batch *batch, const sister_rig *rigs, int nrigs);
-/* Device bytes one rig holds while it is computed when nmodes of its outputs are requested (the modes share
- * the aggregation volumes; BGR input counted). */
+/* Device bytes one rig takes inside a batch when nmodes of its outputs are requested (each mode has its own
+ * aggregation volumes, since a wave aggregates all of them in one launch; BGR input counted). */
 SISTER_API size_t sister_batch_rig_bytes(int width, int height, int max_disparity, int nmodes);
 
 /* --- serving loop ------------------------------------------------------------------------------------

@@ -1,4 +1,4 @@
-// Request engine: continuous admission of independent rigs (the serving loop's requests, a batch's rigs).
+// Request engine of the serving loop: continuous admission of independent rigs (requests).
 //
 // A request is admitted as soon as a stream slot is free and its device memory fits the budget next to the
 // rigs already admitted -- not when an earlier group of requests has finished. Each admitted rig then runs the

@@ -1,4 +1,4 @@
-// Request engine shared by the serving loop (sister_server_*) and the batch path (sister_batch_*): continuous
+// Request engine of the serving loop (sister_server_*): continuous
 // admission of independent rigs against a device-memory budget, each admitted rig computed on its own stream.
 #pragma once
 
