@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 METRIC = "5-view Gpix·disp/s and served p50/p99 latency, batched vs plain GPU, bit-exact"
 UNIT = "Gpix*disp/s"
 W_, H_, DC = 1920, 1080, 256
+SGM_ROWS = 0  # band height forced on the plain leg (--sgm-rows); 0 lets the planner choose
 SEED = 2
 CONFIG = {
     "workload": "plain single rig: 5 views 1920x1080 u8, maxdisp 256, multiview output (mode 0)",
@@ -448,6 +449,8 @@ def run_gb300(args):
     ctx.set_stream(stream.cuda_stream)
     ctx.load_views_device([t.data_ptr() for t in dev_views], w, h, w, 1)
     ctx.set_max_disparity(dc)
+    if SGM_ROWS:
+        ctx.tune_set(sg.TUNE_SGM_ROWS, SGM_ROWS)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     # parity guard: the first result must be bit-exact with the reference's golden output
@@ -648,7 +651,13 @@ def main():
     ap.add_argument("--no-modes3", action="store_true", help="skip the three-output compute_disparities key")
     ap.add_argument("--no-c1", action="store_true", help="skip the 640x480/192 key")
     ap.add_argument("--rig", default=None, help="WxHxDC instead of 1920x1080x256 (profiling of smaller cases)")
+    ap.add_argument("--sgm-rows", type=int, default=0,
+                    help="band height of the plain leg's aggregation (0: the planner's choice; profiling)")
     args = ap.parse_args()
+    if args.sgm_rows:
+        global SGM_ROWS
+        SGM_ROWS = args.sgm_rows
+        CONFIG["sgm_rows"] = SGM_ROWS
     if args.rig:
         global W_, H_, DC
         W_, H_, DC = (int(v) for v in args.rig.lower().split("x"))

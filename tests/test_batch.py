@@ -58,6 +58,39 @@ def test_batch_matches_single_rig_path(gpu_lib):
     b.close()
 
 
+def test_batch_matches_oracle(gpu_lib, port):
+    """The batched outputs against the oracle directly (not only through the single-rig path): every gray rig of
+    the mix, in every mode it asks for, in one batch."""
+    rigs = [r for r, spec in zip(_rigs(seed0=90), MIX) if not spec[6]]
+    b = sg.Batch(0, 0)
+    got = b.run(rigs)
+    b.close()
+    for k, ((views, dc, modes), g) in enumerate(zip(rigs, got)):
+        want = port.compute(views, dc, modes=modes)
+        for m in range(3):
+            if modes[m]:
+                assert np.array_equal(g[m], want[m]), "rig %d mode %d: %d px differ" % (
+                    k, m, int((g[m] != want[m]).sum()))
+
+
+def test_batch_benchmark_shapes_match_oracle(gpu_lib, port):
+    """The four smallest rigs of the benchmarked 64-rig uneven batch (same shapes and seeds as its batched leg),
+    batched together with two of its larger rigs, against the oracle: the benchmark's own shapes meet the oracle,
+    not only the single-rig path."""
+    shapes = synth.batch_shapes(64, seed=3)
+    cells = [((w + 2 * dc) * (h + 2 * dc) * dc, k) for k, (w, h, dc) in enumerate(shapes)]
+    pick = [k for _, k in sorted(cells)[:4]] + [k for _, k in sorted(cells)[30:32]]
+    rigs = [synth.rig_for_shape(*shapes[k], seed=1000 + k) for k in pick]
+    b = sg.Batch(0, 0)
+    got = b.run([(views, dc) for (views, _), dc in rigs])
+    b.close()
+    for k, (((views, _), dc), g) in enumerate(zip(rigs, got)):
+        if k >= 4:
+            continue  # the larger rigs only share the batch; the oracle checks the four small ones
+        want = port.compute(views, dc, modes=(True, False, False))[0]
+        assert np.array_equal(g[0], want), "shape %s: %d px differ" % (shapes[pick[k]], int((g[0] != want).sum()))
+
+
 def test_batch_waves_under_a_small_budget(gpu_lib):
     rigs = _rigs(seed0=70)
     want = [_single(r) for r in rigs]

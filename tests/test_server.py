@@ -32,9 +32,11 @@ def _single(views, dc, modes=(True, False, False)):
     return out
 
 
-def test_server_concurrent_submitters_match_single_rig_path(gpu_lib):
+def test_server_concurrent_submitters_match_single_rig_path(gpu_lib, port):
     rigs = [_rig(k) for k in range(len(SHAPES))]
     want = [_single(v, dc)[0] for v, dc in rigs]
+    for k, (v, dc) in enumerate(rigs):  # the single-rig path itself against the oracle for these shapes
+        assert np.array_equal(want[k], port.compute(v, dc, modes=(True, False, False))[0]), "rig %d" % k
     srv = sg.Server(0, 1 << 30)
     tickets = [None] * len(rigs)
 
