@@ -15,7 +15,8 @@ namespace {
 //
 // A CTA computes an 8x8 tile of padded pixels. The transposed frames 1 and 3 read one frame row per tile column
 // (a column of the padded image), so their neighbour census windows (dp + 10 words per tile column) are staged in
-// shared memory first and each word is fetched from L2/HBM once per tile instead of once per pixel; frames 0 and 2
+// shared memory first (2 x 8 x (dp + 10) words: 34 KB at dp = 256, six CTAs per SM; 67 KB at dp = 512, three) and
+// each word is fetched from L2/HBM once per tile instead of once per pixel; frames 0 and 2
 // read one contiguous stretch of their census row per tile row, which consecutive pixels share through L1. Each
 // pixel's centre words and frame states (masked, constant row, or its column b) are staged too. Then warp w
 // computes the 8 pixels of tile row w, one at a time, lanes over d (lane l holds d = l + 32k, k < DPL). Frames whose
@@ -161,69 +162,9 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     }
 }
 
-// Wide disparity strides (dp > 256): the staged windows of a tile would take more than half of an SM's shared
-// memory (134 KB at dp = 512, one CTA per SM), so these use one warp per pixel instead, gathering the census
-// words from L1/L2: 8 pixels of one row per CTA, CTAs ordered row-fastest so that consecutive CTAs share the
-// transposed frames' rows, and the frame loop outside the disparity loop so that each frame's loads issue together.
-template <int DPL>
-__global__ void __launch_bounds__(256) masked_cost_gather_kernel(const uint64_t *__restrict__ census,
-                                                          const uint8_t *__restrict__ masks, Geom g, int mode,
-                                                          uint16_t *__restrict__ cost) {
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int i = blockIdx.x, j = blockIdx.y * 8 + wp;
-    if (j >= g.Wp) return;
-    const size_t p = (size_t)i * g.Wp + j;
-    const int D = g.dc;
-    uint32_t acc[DPL];
-#pragma unroll
-    for (int k = 0; k < DPL; k++) acc[k] = 0;
-#pragma unroll
-    for (int f = 0; f < 4; f++) {
-        const bool in_mode = (mode == 0) || (mode == 1 && !(f & 1)) || (mode == 2 && (f & 1)) || (mode == 3 && f == 0);
-        if (!in_mode || (mode != 3 && !masks[(size_t)f * g.plane + p])) continue; // warp-uniform
-        int fa, fb;
-        switch (f) {
-        case 0: fa = i; fb = j; break;
-        case 2: fa = i; fb = g.Wp - 1 - j; break;
-        case 1: fa = g.Wp - 1 - j; fb = g.Hp - 1 - i; break;
-        default: fa = g.Wp - 1 - j; fb = i; break;
-        }
-        const int fh = g.frows(f), fw = g.fcols(f);
-        if (fa < 3 || fa >= fh - 2) { // whole frame row constant: 255 (rows 0..2) or 0 (never written)
-            const uint32_t c = fa < 3 ? 255u : 0u;
-#pragma unroll
-            for (int k = 0; k < DPL; k++) acc[k] += c;
-            continue;
-        }
-        const uint64_t cc = census[(size_t)(2 * f) * g.plane + (size_t)fa * fw + fb];
-        const uint64_t *cn = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa * fw + fb;
-        uint64_t wv[DPL];
-#pragma unroll
-        for (int k = 0; k < DPL; k++) {
-            const int d = lane + 32 * k;
-            wv[k] = (d <= fb && d < D) ? __ldg(cn - d) : 0;
-        }
-#pragma unroll
-        for (int k = 0; k < DPL; k++) {
-            const int d = lane + 32 * k;
-            acc[k] += d > fb ? 255u : (uint32_t)__popcll(cc ^ wv[k]);
-        }
-    }
-    uint16_t *out = cost + p * g.dp;
-#pragma unroll
-    for (int k = 0; k < DPL; k++) {
-        const int d = lane + 32 * k;
-        out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
-    }
-}
-
 template <int DPL>
 void launch_cost_dpl(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                      cudaStream_t st) {
-    if (g.dp > 256) {
-        masked_cost_gather_kernel<DPL><<<dim3(g.Hp, (g.Wp + 7) / 8), 256, 0, st>>>(census, masks, g, mode, cost);
-        return;
-    }
     dim3 grid((g.Wp + kCostTile - 1) / kCostTile, (g.Hp + kCostTile - 1) / kCostTile);
     const size_t smem = (size_t)2 * kCostTile * cost_win(g.dp) * sizeof(uint64_t);
     masked_cost_kernel<DPL><<<grid, 256, smem, st>>>(census, masks, g, mode, cost);
