@@ -13,17 +13,17 @@ namespace {
 // The volume is stored with d-stride dp; entries d >= dc hold 0x7FFF, the aggregation's infinite cost
 // (large enough never to win a minimum, small enough that packed 16-bit updates cannot wrap).
 //
-// A CTA computes an 8x8 tile of padded pixels. The transposed frames 1 and 3 read one frame row per tile column
-// (a column of the padded image), so their neighbour census windows (dp + 10 words per tile column) are staged in
-// shared memory first (2 x 8 x (dp + 10) words: 34 KB at dp = 256, six CTAs per SM; 67 KB at dp = 512, three) and
-// each word is fetched from L2/HBM once per tile instead of once per pixel; frames 0 and 2
-// read one contiguous stretch of their census row per tile row, which consecutive pixels share through L1. Each
+// A CTA computes a tile of 8 rows x TW columns of padded pixels (TW = 4 or 8). The transposed frames 1 and 3 read
+// one frame row per tile column (a column of the padded image), so their neighbour census windows (dp + 10 words
+// per tile column, 2 x TW windows) are staged in shared memory first and each word is fetched from L2/HBM once per
+// tile instead of once per pixel; frames 0 and 2 read one contiguous stretch of their census row per tile row,
+// which consecutive pixels share through L1. Each
 // pixel's centre words and frame states (masked, constant row, or its column b) are staged too. Then warp w
-// computes the 8 pixels of tile row w, one at a time, lanes over d (lane l holds d = l + 32k, k < DPL). Frames whose
+// computes the TW pixels of tile row w, one at a time, lanes over d (lane l holds d = l + 32k, k < DPL). Frames whose
 // column b >= dp-1 (most of them) need no per-lane d > b test; nearer the left edge the test is one warp-uniform
 // branch per k. Summing the four frames' XOR words with carry-save adders before counting (5 popcounts instead
 // of 8 per d) was slower in every form tried (2.2-3.5 ms against 1.40): the popcount pipe is not the limit.
-constexpr int kCostTile = 8;
+constexpr int kCostRows = 8; // tile rows: one warp each
 constexpr int kNoCost = -3, kRow255 = -2, kRow0 = -1; // per-pixel frame states besides b >= 0
 __host__ __device__ inline int cost_win(int dp) { return dp + 10; } // words per staged frame row (even)
 __host__ __device__ inline bool cost_in_mode(int mode, int f) {
@@ -31,32 +31,33 @@ __host__ __device__ inline bool cost_in_mode(int mode, int f) {
 }
 // first (even) column of the window of tile row r of frame f: it covers every b - d with b in the tile and
 // 0 <= d < dp
+template <int TW>
 __device__ __forceinline__ int cost_win0(const Geom &g, int f, int i0, int j0) {
     int c0;
     switch (f) {
     case 0: c0 = j0 - g.dp; break;                        // b = j
-    case 2: c0 = g.Wp - j0 - (kCostTile - 1) - g.dp; break; // b = Wp-1-j
-    case 1: c0 = g.Hp - i0 - (kCostTile - 1) - g.dp; break; // b = Hp-1-i
+    case 2: c0 = g.Wp - j0 - (TW - 1) - g.dp; break;       // b = Wp-1-j
+    case 1: c0 = g.Hp - i0 - (kCostRows - 1) - g.dp; break; // b = Hp-1-i
     default: c0 = i0 - g.dp; break;                         // b = i
     }
     return c0 & ~1;
 }
 
-template <int DPL>
+template <int DPL, int TW>
 __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__restrict__ census,
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
                                                           uint16_t *__restrict__ cost) {
     extern __shared__ __align__(16) uint64_t win[]; // [frame 1, 3][tile column][cost_win(dp)]
     // per frame and tile pixel: the centre census word, or kNoCost when the pixel's frame is unused (out of the
     // mode or masked) and kRow255 / kRow0 when its frame row is constant
-    __shared__ uint64_t ctr[4][kCostTile * kCostTile];
-    __shared__ int fbs[4][kCostTile * kCostTile];
+    __shared__ uint64_t ctr[4][kCostRows * TW];
+    __shared__ int fbs[4][kCostRows * TW];
     const int nwin = cost_win(g.dp);
-    const int i0 = blockIdx.y * kCostTile, j0 = blockIdx.x * kCostTile;
+    const int i0 = blockIdx.y * kCostRows, j0 = blockIdx.x * TW;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int e = threadIdx.x; e < 4 * kCostTile * kCostTile; e += blockDim.x) {
-        const int f = e / (kCostTile * kCostTile), t = e % (kCostTile * kCostTile);
-        const int i = i0 + t / kCostTile, j = j0 + t % kCostTile;
+    for (int e = threadIdx.x; e < 4 * kCostRows * TW; e += blockDim.x) {
+        const int f = e / (kCostRows * TW), t = e % (kCostRows * TW);
+        const int i = i0 + t / TW, j = j0 + t % TW;
         int fb = kNoCost;
         uint64_t c = 0;
         if (i < g.Hp && j < g.Wp && cost_in_mode(mode, f) &&
@@ -75,16 +76,16 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
         fbs[f][t] = fb;
         ctr[f][t] = c;
     }
-    // ---- stage the transposed frames' windows: warp w copies staged rows w and w+8 (frame 1 then 3, tile column
-    // q % 8: frame row Wp-1-(j0+r)) with 16-byte asynchronous copies (windows start on even columns, frame rows on
+    // ---- stage the transposed frames' windows: warp w copies staged rows q = w, w+8, ... < 2 TW (frame 1 then 3,
+    // tile column r = q % TW: frame row Wp-1-(j0+r)) with 16-byte asynchronous copies (windows start on even columns, frame rows on
     // 16-byte boundaries); columns outside the frame row are never read and stay unwritten. Frames 0 and 2 need one
     // contiguous stretch of their census row per tile row, read through L1 by the warps themselves.
-    for (int q = w; q < 2 * kCostTile; q += 8) {
-        const int f = q < kCostTile ? 1 : 3, r = q % kCostTile;
+    for (int q = w; q < 2 * TW; q += kCostRows) {
+        const int f = q < TW ? 1 : 3, r = q % TW;
         if (!cost_in_mode(mode, f)) continue;
         const int fa = g.Wp - 1 - (j0 + r);
         if (fa < 0 || fa >= g.frows(f)) continue;
-        const int c0 = cost_win0(g, f, i0, j0), fw = g.fcols(f);
+        const int c0 = cost_win0<TW>(g, f, i0, j0), fw = g.fcols(f);
         const uint64_t *src = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa * fw;
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(win + (size_t)q * nwin);
         for (int u = lane; u < nwin / 2; u += 32) {
@@ -104,8 +105,8 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     // 3 the staged window of tile column jj
     const uint64_t *grow0 = census + (size_t)1 * g.plane + (size_t)i * g.Wp; // frame 0 (fa = i)
     const uint64_t *grow2 = census + (size_t)5 * g.plane + (size_t)i * g.Wp; // frame 2 (fa = i)
-    const int sw1 = -cost_win0(g, 1, i0, j0), sw3 = kCostTile * nwin - cost_win0(g, 3, i0, j0);
-    for (int jj = 0; jj < kCostTile; jj++) {
+    const int sw1 = -cost_win0<TW>(g, 1, i0, j0), sw3 = TW * nwin - cost_win0<TW>(g, 3, i0, j0);
+    for (int jj = 0; jj < TW; jj++) {
         const int j = j0 + jj;
         if (j >= g.Wp) break;
         const size_t p = (size_t)i * g.Wp + j;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
         for (int k = 0; k < DPL; k++) acc[k] = 0;
 #pragma unroll
         for (int f = 0; f < 4; f++) {
-            const int t = w * kCostTile + jj;
+            const int t = w * TW + jj;
             const int fb = fbs[f][t]; // warp-uniform
             if (fb == kNoCost) continue;
             if (fb < 0) {
@@ -162,12 +163,19 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     }
 }
 
+// tile width (columns) of the cost kernel for a d-stride: the staged windows take 2 x TW x (dp + 10) words. Four
+// columns from dp = 256 up (17 KB at 256: eight CTAs per SM; 33 KB at 512: six), measured against eight: 1.10 ->
+// 1.05 ms at 1920x1080/256, 14.2 -> 12.0 ms at 4096x3000/512; below 256 eight columns stay ahead by ~2%.
+template <int DPL>
+constexpr int cost_tw() { return 32 * DPL >= 256 ? 4 : 8; }
+
 template <int DPL>
 void launch_cost_dpl(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                      cudaStream_t st) {
-    dim3 grid((g.Wp + kCostTile - 1) / kCostTile, (g.Hp + kCostTile - 1) / kCostTile);
-    const size_t smem = (size_t)2 * kCostTile * cost_win(g.dp) * sizeof(uint64_t);
-    masked_cost_kernel<DPL><<<grid, 256, smem, st>>>(census, masks, g, mode, cost);
+    constexpr int TW = cost_tw<DPL>();
+    dim3 grid((g.Wp + TW - 1) / TW, (g.Hp + kCostRows - 1) / kCostRows);
+    const size_t smem = (size_t)2 * TW * cost_win(g.dp) * sizeof(uint64_t);
+    masked_cost_kernel<DPL, TW><<<grid, 256, smem, st>>>(census, masks, g, mode, cost);
 }
 
 template <int DPL>
@@ -175,9 +183,10 @@ void set_cost_attr() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    constexpr int TW = cost_tw<DPL>();
     cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, masked_cost_kernel<DPL>);
-    cudaFuncSetAttribute(masked_cost_kernel<DPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncGetAttributes(&fa, masked_cost_kernel<DPL, TW>);
+    cudaFuncSetAttribute(masked_cost_kernel<DPL, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          optin - (int)fa.sharedSizeBytes); // the static part counts against the limit too
 }
 
