@@ -23,40 +23,42 @@ namespace {
 // column b >= dp-1 (most of them) need no per-lane d > b test; nearer the left edge the test is one warp-uniform
 // branch per k. Summing the four frames' XOR words with carry-save adders before counting (5 popcounts instead
 // of 8 per d) was slower in every form tried (2.2-3.5 ms against 1.40): the popcount pipe is not the limit.
-constexpr int kCostRows = 8; // tile rows: one warp each
+constexpr int kCostWarps = 8; // warps per CTA; warp w computes tile rows w, w + 8, ...
 constexpr int kNoCost = -3, kRow255 = -2, kRow0 = -1; // per-pixel frame states besides b >= 0
-__host__ __device__ inline int cost_win(int dp) { return dp + 10; } // words per staged frame row (even)
+// words per staged frame row of a tile of RW rows (even): every b - d with d < dp for the tile's RW values of b, plus
+// the rounding of the window's start down to an even column
+__host__ __device__ inline int cost_win(int dp, int RW) { return dp + RW + 2; }
 __host__ __device__ inline bool cost_in_mode(int mode, int f) {
     return mode == 0 || (mode == 1 && !(f & 1)) || (mode == 2 && (f & 1)) || (mode == 3 && f == 0);
 }
 // first (even) column of the window of tile row r of frame f: it covers every b - d with b in the tile and
 // 0 <= d < dp
-template <int TW>
+template <int TW, int RW>
 __device__ __forceinline__ int cost_win0(const Geom &g, int f, int i0, int j0) {
     int c0;
     switch (f) {
     case 0: c0 = j0 - g.dp; break;                        // b = j
     case 2: c0 = g.Wp - j0 - (TW - 1) - g.dp; break;       // b = Wp-1-j
-    case 1: c0 = g.Hp - i0 - (kCostRows - 1) - g.dp; break; // b = Hp-1-i
+    case 1: c0 = g.Hp - i0 - (RW - 1) - g.dp; break;       // b = Hp-1-i
     default: c0 = i0 - g.dp; break;                         // b = i
     }
     return c0 & ~1;
 }
 
-template <int DPL, int TW>
+template <int DPL, int TW, int RW>
 __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__restrict__ census,
                                                           const uint8_t *__restrict__ masks, Geom g, int mode,
                                                           uint16_t *__restrict__ cost) {
     extern __shared__ __align__(16) uint64_t win[]; // [frame 1, 3][tile column][cost_win(dp)]
     // per frame and tile pixel: the centre census word, or kNoCost when the pixel's frame is unused (out of the
     // mode or masked) and kRow255 / kRow0 when its frame row is constant
-    __shared__ uint64_t ctr[4][kCostRows * TW];
-    __shared__ int fbs[4][kCostRows * TW];
-    const int nwin = cost_win(g.dp);
-    const int i0 = blockIdx.y * kCostRows, j0 = blockIdx.x * TW;
+    __shared__ uint64_t ctr[4][RW * TW];
+    __shared__ int fbs[4][RW * TW];
+    const int nwin = cost_win(g.dp, RW);
+    const int i0 = blockIdx.y * RW, j0 = blockIdx.x * TW;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int e = threadIdx.x; e < 4 * kCostRows * TW; e += blockDim.x) {
-        const int f = e / (kCostRows * TW), t = e % (kCostRows * TW);
+    for (int e = threadIdx.x; e < 4 * RW * TW; e += blockDim.x) {
+        const int f = e / (RW * TW), t = e % (RW * TW);
         const int i = i0 + t / TW, j = j0 + t % TW;
         int fb = kNoCost;
         uint64_t c = 0;
@@ -80,12 +82,12 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     // tile column r = q % TW: frame row Wp-1-(j0+r)) with 16-byte asynchronous copies (windows start on even columns, frame rows on
     // 16-byte boundaries); columns outside the frame row are never read and stay unwritten. Frames 0 and 2 need one
     // contiguous stretch of their census row per tile row, read through L1 by the warps themselves.
-    for (int q = w; q < 2 * TW; q += kCostRows) {
+    for (int q = w; q < 2 * TW; q += kCostWarps) {
         const int f = q < TW ? 1 : 3, r = q % TW;
         if (!cost_in_mode(mode, f)) continue;
         const int fa = g.Wp - 1 - (j0 + r);
         if (fa < 0 || fa >= g.frows(f)) continue;
-        const int c0 = cost_win0<TW>(g, f, i0, j0), fw = g.fcols(f);
+        const int c0 = cost_win0<TW, RW>(g, f, i0, j0), fw = g.fcols(f);
         const uint64_t *src = census + (size_t)(2 * f + 1) * g.plane + (size_t)fa * fw;
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(win + (size_t)q * nwin);
         for (int u = lane; u < nwin / 2; u += 32) {
@@ -97,67 +99,69 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
     }
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-    // ---- warp w: tile row w
-    const int i = i0 + w;
-    if (i >= g.Hp) return;
+    // ---- warp w: tile rows w, w + 8, ...
     const int D = g.dc;
-    // neighbour census row of each frame, indexed by the column b - d: frames 0 and 2 the global row i, frames 1 and
-    // 3 the staged window of tile column jj
-    const uint64_t *grow0 = census + (size_t)1 * g.plane + (size_t)i * g.Wp; // frame 0 (fa = i)
-    const uint64_t *grow2 = census + (size_t)5 * g.plane + (size_t)i * g.Wp; // frame 2 (fa = i)
-    const int sw1 = -cost_win0<TW>(g, 1, i0, j0), sw3 = TW * nwin - cost_win0<TW>(g, 3, i0, j0);
-    for (int jj = 0; jj < TW; jj++) {
-        const int j = j0 + jj;
-        if (j >= g.Wp) break;
-        const size_t p = (size_t)i * g.Wp + j;
-        uint32_t acc[DPL];
+    const int sw1 = -cost_win0<TW, RW>(g, 1, i0, j0), sw3 = TW * nwin - cost_win0<TW, RW>(g, 3, i0, j0);
+    for (int rr = w; rr < RW; rr += kCostWarps) {
+        const int i = i0 + rr;
+        if (i >= g.Hp) return;
+        // neighbour census row of each frame, indexed by the column b - d: frames 0 and 2 the global row i, frames 1 and
+        // 3 the staged window of tile column jj
+        const uint64_t *grow0 = census + (size_t)1 * g.plane + (size_t)i * g.Wp; // frame 0 (fa = i)
+        const uint64_t *grow2 = census + (size_t)5 * g.plane + (size_t)i * g.Wp; // frame 2 (fa = i)
+        for (int jj = 0; jj < TW; jj++) {
+            const int j = j0 + jj;
+            if (j >= g.Wp) break;
+            const size_t p = (size_t)i * g.Wp + j;
+            uint32_t acc[DPL];
 #pragma unroll
-        for (int k = 0; k < DPL; k++) acc[k] = 0;
+            for (int k = 0; k < DPL; k++) acc[k] = 0;
 #pragma unroll
-        for (int f = 0; f < 4; f++) {
-            const int t = w * TW + jj;
-            const int fb = fbs[f][t]; // warp-uniform
-            if (fb == kNoCost) continue;
-            if (fb < 0) {
-                const uint32_t c = fb == kRow255 ? 255u : 0u;
+            for (int f = 0; f < 4; f++) {
+                const int t = rr * TW + jj;
+                const int fb = fbs[f][t]; // warp-uniform
+                if (fb == kNoCost) continue;
+                if (fb < 0) {
+                    const uint32_t c = fb == kRow255 ? 255u : 0u;
 #pragma unroll
-                for (int k = 0; k < DPL; k++) acc[k] += c;
-                continue;
-            }
-            const uint64_t cc = ctr[f][t];
-            const uint64_t *wr = (f == 0) ? grow0 + fb
-                                 : (f == 2) ? grow2 + fb
-                                 : win + (jj * nwin + (f == 1 ? sw1 : sw3) + fb);
-            if (fb >= g.dp - 1) { // every d of the stride has its word (d >= dc reads one that is never used)
+                    for (int k = 0; k < DPL; k++) acc[k] += c;
+                    continue;
+                }
+                const uint64_t cc = ctr[f][t];
+                const uint64_t *wr = (f == 0) ? grow0 + fb
+                                     : (f == 2) ? grow2 + fb
+                                     : win + (jj * nwin + (f == 1 ? sw1 : sw3) + fb);
+                if (fb >= g.dp - 1) { // every d of the stride has its word (d >= dc reads one that is never used)
 #pragma unroll
-                for (int k = 0; k < DPL; k++) acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
-            } else {
-                // d = lane + 32k: every lane has d <= b below k = b / 32 and none above it (warp-uniform), so only
-                // that one k tests per lane; d > b costs 255 (census.cpp:74-78)
-                const int kb = fb >> 5;
+                    for (int k = 0; k < DPL; k++) acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
+                } else {
+                    // d = lane + 32k: every lane has d <= b below k = b / 32 and none above it (warp-uniform), so only
+                    // that one k tests per lane; d > b costs 255 (census.cpp:74-78)
+                    const int kb = fb >> 5;
 #pragma unroll
-                for (int k = 0; k < DPL; k++) {
-                    if (k < kb) {
-                        acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
-                    } else if (k == kb) {
-                        const int d = lane + 32 * k; // the load stays inside the row: column b - min(d, b) >= 0
-                        const uint32_t h = (uint32_t)__popcll(cc ^ wr[-min(d, fb)]);
-                        acc[k] += d <= fb ? h : 255u;
-                    } else {
-                        acc[k] += 255u;
+                    for (int k = 0; k < DPL; k++) {
+                        if (k < kb) {
+                            acc[k] += (uint32_t)__popcll(cc ^ wr[-(lane + 32 * k)]);
+                        } else if (k == kb) {
+                            const int d = lane + 32 * k; // the load stays inside the row: column b - min(d, b) >= 0
+                            const uint32_t h = (uint32_t)__popcll(cc ^ wr[-min(d, fb)]);
+                            acc[k] += d <= fb ? h : 255u;
+                        } else {
+                            acc[k] += 255u;
+                        }
                     }
                 }
             }
-        }
-        uint16_t *out = cost + p * g.dp;
-        if (D == g.dp) { // every d of the stride is real
+            uint16_t *out = cost + p * g.dp;
+            if (D == g.dp) { // every d of the stride is real
 #pragma unroll
-            for (int k = 0; k < DPL; k++) out[lane + 32 * k] = (uint16_t)acc[k];
-        } else {
+                for (int k = 0; k < DPL; k++) out[lane + 32 * k] = (uint16_t)acc[k];
+            } else {
 #pragma unroll
-            for (int k = 0; k < DPL; k++) {
-                const int d = lane + 32 * k;
-                out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
+                for (int k = 0; k < DPL; k++) {
+                    const int d = lane + 32 * k;
+                    out[d] = d < D ? (uint16_t)acc[k] : (uint16_t)0x7FFF;
+                }
             }
         }
     }
@@ -168,14 +172,18 @@ __global__ void __launch_bounds__(256) masked_cost_kernel(const uint64_t *__rest
 // 1.05 ms at 1920x1080/256, 14.2 -> 12.0 ms at 4096x3000/512; below 256 eight columns stay ahead by ~2%.
 template <int DPL>
 constexpr int cost_tw() { return 32 * DPL >= 256 ? 4 : 8; }
+// tile rows (16 rows x 4 columns measured slower: 1.08 ms at 1920x1080/256, 13.1 ms at 4096x3000/512; 2 columns
+// slower still)
+template <int DPL>
+constexpr int cost_rw() { return 8; }
 
 template <int DPL>
 void launch_cost_dpl(const uint64_t *census, const uint8_t *masks, const Geom &g, int mode, uint16_t *cost,
                      cudaStream_t st) {
-    constexpr int TW = cost_tw<DPL>();
-    dim3 grid((g.Wp + TW - 1) / TW, (g.Hp + kCostRows - 1) / kCostRows);
-    const size_t smem = (size_t)2 * TW * cost_win(g.dp) * sizeof(uint64_t);
-    masked_cost_kernel<DPL, TW><<<grid, 256, smem, st>>>(census, masks, g, mode, cost);
+    constexpr int TW = cost_tw<DPL>(), RW = cost_rw<DPL>();
+    dim3 grid((g.Wp + TW - 1) / TW, (g.Hp + RW - 1) / RW);
+    const size_t smem = (size_t)2 * TW * cost_win(g.dp, RW) * sizeof(uint64_t);
+    masked_cost_kernel<DPL, TW, RW><<<grid, 32 * kCostWarps, smem, st>>>(census, masks, g, mode, cost);
 }
 
 template <int DPL>
@@ -183,10 +191,10 @@ void set_cost_attr() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    constexpr int TW = cost_tw<DPL>();
+    constexpr int TW = cost_tw<DPL>(), RW = cost_rw<DPL>();
     cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, masked_cost_kernel<DPL, TW>);
-    cudaFuncSetAttribute(masked_cost_kernel<DPL, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncGetAttributes(&fa, masked_cost_kernel<DPL, TW, RW>);
+    cudaFuncSetAttribute(masked_cost_kernel<DPL, TW, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          optin - (int)fa.sharedSizeBytes); // the static part counts against the limit too
 }
 
