@@ -70,7 +70,9 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi samples (every 200 ms) during the timed region."""
+    """nvidia-smi samples every 50 ms, read by a thread with their arrival times. start() returns once the first
+    sample has arrived (so sampling covers the timed region), mark() brackets the timed region, and stop() keeps the
+    samples that arrived inside it (the last sample before it if none did: a region shorter than the interval)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -80,26 +82,50 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
+        self.lines = []
+        self.t0 = self.t1 = None
 
-    def start(self):
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.perf_counter(), line))
+
+    def start(self, wait_s: float = 3.0):
+        import threading
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+        t = time.perf_counter()
+        while not self.lines and time.perf_counter() - t < wait_s:
+            time.sleep(0.01)
+
+    def mark(self, end: bool = False):
+        if end:
+            self.t1 = time.perf_counter()
+        else:
+            self.t0 = time.perf_counter()
 
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        time.sleep(0.06)  # the sample in flight at the end of the region
         self.proc.terminate()
         try:
-            out, _ = self.proc.communicate(timeout=5)
+            self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-            out, _ = self.proc.communicate()
+        t0 = self.t0 if self.t0 is not None else float("-inf")
+        t1 = self.t1 if self.t1 is not None else float("inf")
+        inside = [l for t, l in self.lines if t0 <= t <= t1 + 0.05]
+        if not inside:
+            before = [l for t, l in self.lines if t < t0]
+            inside = before[-1:]
         sm, smax, reasons = [], [], set()
-        for line in out.splitlines():
+        for line in inside:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -262,7 +288,7 @@ def batched_leg(local):
 
 
 def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 2000.0), seconds=2.0,
-               max_queue=32):
+               max_queue=32, max_inflight=8):
     """C4: Poisson arrivals of single-rig requests (mix: 50% 640x480/128, 35% 1920x1080/256, 15% 2448x2048/256)
     into the serving loop with a 16 GB device budget and continuous admission; requests beyond a queue of
     `max_queue` are refused (backpressure). Latency = submission to outputs in host memory (pinned views and
@@ -292,13 +318,13 @@ def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 200
             keep.append(t)
             outs.append(t.numpy().view(np.uint16))
         pools.append((pool, dc, outs))
-    srv = sg.Server(local, 16 << 30, max_inflight=8, max_queue=max_queue)
+    srv = sg.Server(local, 16 << 30, max_inflight=max_inflight, max_queue=max_queue)
     for ci in range(len(mix)):  # warm-up: one of each class
         pool, dc, outs = pools[ci]
         srv.wait(srv.submit(pool[0], dc, outputs=(outs[0],)))
     out = {"workload": "Poisson arrivals, mix 50%% 640x480/128, 35%% 1920x1080/256, 15%% 2448x2048/256, mode 0, "
-                       "16 GB device budget, continuous admission (8 in flight), queue bound %d; %.0f s per rate"
-                       % (max_queue, seconds), "unit": "ms", "rates": []}
+                       "16 GB device budget, continuous admission (%d in flight), queue bound %d; %.0f s per rate"
+                       % (max_inflight, max_queue, seconds), "unit": "ms", "rates": []}
     rnd = random.Random(7)
     for rate in rates:
         sched = []
@@ -467,10 +493,11 @@ def run_gb300(args):
     stage_ms = {}
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler(local)
+    clocks.start()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks.start()
+    clocks.mark()
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -481,6 +508,7 @@ def run_gb300(args):
             stage_ms.setdefault(name, []).append(ms)
     ctx.synchronize()
     torch.cuda.synchronize()
+    clocks.mark(end=True)
     clk = clocks.stop()
     ctx.profile(False)
     total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world)

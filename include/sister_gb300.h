@@ -87,8 +87,9 @@ SISTER_API int sister_set_stream(sister_ctx *ctx, void *stream);
 /* Wait for queued work; reports device-side errors (e.g. SISTER_ETIMEOUT) of completed launches. */
 SISTER_API int sister_synchronize(sister_ctx *ctx);
 
-/* Bytes of device memory the context would hold for a w x h rig at max disparity dc (about 8.3 GB for
- * 1920x1080 at 256: cost and two pass-sum volumes of (w+2dc)(h+2dc)*32*ceil(dc/32) u16 dominate). */
+/* Bytes of device memory the context would hold for one output mode of a w x h rig at max disparity dc (about
+ * 4.6 GB for 1920x1080 at 256: the cost volume of (w+2dc)(h+2dc) pixels and the two pass sums of the w x h
+ * original pixels, 32*ceil(dc/32) u16 each, dominate; SISTER_TUNE_FULL_DISP keeps sums of all padded pixels). */
 SISTER_API size_t sister_device_bytes(int width, int height, int dc);
 
 /* --- aggregation without device allocation ------------------------------------------------ */

@@ -52,6 +52,7 @@ namespace sister {
 constexpr int kHelpers = 3; // fetcher, writer and releaser warps
 constexpr int kKP = 4;      // ring slots of a row read by the row below
 constexpr int kKS = 8;      // ring slots of the band's last row, read by the writer
+constexpr int kBndRows = 2; // global hand-off rows per pass (a power of two), reused by every other band
 // most rows per band (one warp each) by d-stride; shared memory may allow fewer
 __host__ __device__ constexpr int rows_cap(int dp) { return dp <= 256 ? 14 : dp <= 384 ? 12 : 9; }
 // pixels per batched copy: cost group of a row, and records per fetch
@@ -366,7 +367,8 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
         const int nbat = (W + FB - 1) / FB;
         const uint16_t *cost = rg.cost;
         uint16_t *sum = pass ? rg.sum1 : rg.sum0;
-        uint16_t *bnd = rg.bnd + (size_t)pass * rg.nbands * W * rec;
+        // hand-off rows of this pass: band b writes row b & 1, band b+1 reads it (see sgm_bnd_bytes)
+        uint16_t *bnd = rg.bnd + (size_t)pass * kBndRows * W * rec;
         unsigned *progress = rg.progress + (size_t)pass * rg.nbands * kProgressStride;
         const int row0 = band * R;
         const int rows = min(R, H - row0);
@@ -445,7 +447,18 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             uint32_t hm1 = 0;
 #pragma unroll
             for (int k = 0; k < NP; k++) h1[k] = INF2;
-            uint16_t *sp = sum + (rowbase + (pass ? W - 1 : 0)) * dp + d0;
+            // the pass sum is stored for pixels q in [qlo, qhi) of this row, those inside the stored window
+            // (columns sx0 .. sx0+sw-1; pass 1 meets them from the right), at consecutive cells of the volume
+            int sx0 = 0, sy0 = 0, sw = W, sh = H;
+            if (rg.sw) {
+                sx0 = rg.sx0;
+                sy0 = rg.sy0;
+                sw = rg.sw;
+                sh = rg.sh;
+            }
+            const bool row_kept = i >= sy0 && i < sy0 + sh;
+            const int qlo = row_kept ? (pass ? W - sx0 - sw : sx0) : 0, qhi = row_kept ? qlo + sw : 0;
+            uint16_t *sp = row_kept ? sum + ((size_t)(i - sy0) * sw + (pass ? sw - 1 : 0)) * dp + d0 : sum;
             const ptrdiff_t sstep = pass ? -(ptrdiff_t)dp : (ptrdiff_t)dp;
             const uint16_t *cg = myc;
             int cn = 0;
@@ -554,8 +567,10 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                 }
                 // the pass's sum: first line r0 alone (sgm.cpp:132, :187), else r0+r1+r2+r3 (:386-391); u16
                 // arithmetic never saturates or wraps for real disparities
-                stg_stream<NP>(sp, g);
-                sp += sstep;
+                if ((unsigned)(q - qlo) < (unsigned)(qhi - qlo)) {
+                    stg_stream<NP>(sp, g);
+                    sp += sstep;
+                }
                 if (has_cons) {
                     stw<NP>(dst + d0, n1);
                     stw<NP>(dst + dp + d0, n2);
@@ -576,7 +591,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
         } else if (wi == R && band > 0) {
             // ===================================================== fetcher: records of the band above -> inring
             if (lane == 0) {
-                const uint16_t *src = bnd + (size_t)(band - 1) * W * rec;
+                const uint16_t *src = bnd + (size_t)((band - 1) & (kBndRows - 1)) * W * rec;
                 const unsigned *prog = progress + (size_t)(band - 1) * kProgressStride;
                 unsigned seen = 0;
                 for (int b = 0; b < nhb; b++) {
@@ -615,7 +630,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             // record x is complete once the last row has arrived on the slot of x+1 (x = W-1: virtual pixel W).
             // At the end of every hand-off batch the count of copied records goes to the releaser through
             // shared memory; the writer itself never waits on a device-wide fence.
-            uint16_t *dst = bnd + (size_t)band * W * rec;
+            uint16_t *dst = bnd + (size_t)(band & (kBndRows - 1)) * W * rec;
             const uint16_t *lring = rings + (size_t)(R - 1) * kKP * rec;
             const uint32_t lbar = bars + 16u * (uint32_t)((R - 1) * kKP);
             const int nch = rec / 8; // 16-byte chunks per record
@@ -664,7 +679,8 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
 // reads the sum volumes over w*h pixels instead of Wp*Hp.
 template <int DPL>
 __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict__ s0v, const uint16_t *__restrict__ s1v,
-                                                      Geom g, uint16_t *__restrict__ out, uint16_t *__restrict__ disp) {
+                                                      Geom g, uint16_t *__restrict__ out, uint16_t *__restrict__ disp,
+                                                      bool cropped) {
     constexpr int NP = DPL / 2;
     const int lane = threadIdx.x & 31;
     const size_t t = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -679,10 +695,11 @@ __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict
         j = (int)(t % g.w) + g.dc;
     }
     const size_t pix = (size_t)i * g.Wp + j;
+    const size_t cell = cropped ? t : pix; // stored sums: the original image only (row-major, w per row) or the plane
     const int d0 = lane * DPL, D = g.dc;
     uint32_t s0[NP], s1[NP];
-    ldw<NP>(s0v + pix * g.dp + d0, s0);
-    ldw<NP>(s1v + pix * g.dp + d0, s1);
+    ldw<NP>(s0v + cell * g.dp + d0, s0);
+    ldw<NP>(s1v + cell * g.dp + d0, s1);
     // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums are smaller). Pixels
     // with j >= dp-1 in a volume whose stride holds only real disparities (dc = dp) need neither test (warp-uniform)
     uint32_t best = 0xFFFFFFFFu;
@@ -861,8 +878,13 @@ SgmPlan sgm_plan_gb300(const Geom &g) {
     });
 }
 
-size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p) {
-    return (size_t)std::max(p.ngroups, 1) * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
+// Hand-off records: kBndRows rows of Wp records per pass, band b writing row b % kBndRows. Two rows suffice: band
+// b+2 writes record x only after its last row reached pixel x, which trails its first row by R-1 pixels, which
+// trails band b+1's last row, which trails band b+1's first row by R-1 more; so band b+1's first row has passed
+// pixel x + 2R - 1 by then, and it processes a pixel only after its fetcher's copy of that record from band b's row
+// has landed in shared memory. (An expired wait breaks the chain, but then the result is reported as a timeout.)
+size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &) {
+    return (size_t)2 * kBndRows * g.Wp * rec_u16(g.dp) * sizeof(uint16_t);
 }
 
 cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
@@ -935,15 +957,16 @@ cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16
 }
 
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *out, uint16_t *disp,
-                           cudaStream_t st) {
+                           cudaStream_t st, bool cropped) {
+    if (cropped && disp) return cudaErrorInvalidValue; // a padded map needs the sums of the whole plane
     const unsigned blocks = (unsigned)(((disp ? g.plane : (size_t)g.w * g.h) + 7) / 8);
     switch (g.dpl) {
-    case 2: sgm_wta_kernel<2><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
-    case 4: sgm_wta_kernel<4><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
-    case 6: sgm_wta_kernel<6><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
-    case 8: sgm_wta_kernel<8><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
-    case 12: sgm_wta_kernel<12><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
-    case 16: sgm_wta_kernel<16><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp); break;
+    case 2: sgm_wta_kernel<2><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
+    case 4: sgm_wta_kernel<4><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
+    case 6: sgm_wta_kernel<6><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
+    case 8: sgm_wta_kernel<8><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
+    case 12: sgm_wta_kernel<12><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
+    case 16: sgm_wta_kernel<16><<<blocks, 256, 0, st>>>(s0, s1, g, out, disp, cropped); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -112,7 +112,7 @@ extern "C" int sister_aggregate_static(const uint16_t *cost, int width, int heig
     // counters are cleared by the aggregation launch)
     cudaError_t e = cudaMemsetAsync(errflag, 0, sizeof(unsigned), st);
     if (e == cudaSuccess) e = launch_sgm(g, p, a, errflag, st);
-    if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, out, disp_padded, st);
+    if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, out, disp_padded, st, false); // whole-plane sums
     unsigned flag = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, errflag, sizeof flag, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -91,6 +91,7 @@ struct sister_ctx {
     }
     int last_mode = -1;
     const uint16_t *last_cost = nullptr, *last_sum0 = nullptr; // volumes of the last aggregated mode
+    bool last_cropped = false; // whether last_sum0 holds only the original image's pixels
     bool have_intermediates = false;
     Geom g{};
 
@@ -192,12 +193,12 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
         {&c->med, 8 * plane * sizeof(uint16_t), "median"},
         {&c->masks, 4 * plane, "masks"},
         {&c->cost, vol * sizeof(uint16_t), "cost volume"},
-        {&c->sum0, vol * sizeof(uint16_t), "pass-0 sum volume"},
-        {&c->sum1, vol * sizeof(uint16_t), "pass-1 sum volume"},
+        {&c->sum0, sgm_sum_cells(g, !c->full_disp) * sizeof(uint16_t), "pass-0 sum volume"},
+        {&c->sum1, sgm_sum_cells(g, !c->full_disp) * sizeof(uint16_t), "pass-1 sum volume"},
         {&c->bnd, sgm_bnd_bytes(g, p), "band boundary states"},
         {&c->progress, sgm_progress_bytes(std::max(p.ngroups, 1)), "progress"},
         {&c->errflag, sizeof(unsigned), "error flag"},
-        {&c->disp, 3 * plane * sizeof(uint16_t), "disparity"},
+        {&c->disp, (c->full_disp ? 3 * plane : 1) * sizeof(uint16_t), "disparity"},
         {&c->outs, 3 * (size_t)g.w * g.h * sizeof(uint16_t), "outputs"},
     };
     for (auto &r : req) {
@@ -224,9 +225,10 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
             modes[nm++] = m;
             mask |= 1 << m;
         }
-    const size_t vol = g.plane * g.dp * sizeof(uint16_t), bnd = sgm_bnd_bytes(g, plan);
-    const size_t prog = sgm_progress_bytes(std::max(plan.ngroups, 1));
-    const size_t per = 3 * vol + bnd + prog; // cost, sum0, sum1, hand-off records, progress counters
+    const bool cropped = !c->full_disp; // the pass sums of the original image only, unless the padded map is kept
+    const size_t vol = g.plane * g.dp * sizeof(uint16_t), svol = sgm_sum_cells(g, cropped) * sizeof(uint16_t);
+    const size_t bnd = sgm_bnd_bytes(g, plan), prog = sgm_progress_bytes(std::max(plan.ngroups, 1));
+    const size_t per = vol + 2 * svol + bnd + prog; // cost, sum0, sum1, hand-off records, progress counters
     cudaError_t e = c->modevols.ensure((size_t)(nm - 1) * per);
     if (e != cudaSuccess) return c->cuda_fail(e, "per-mode volumes");
     SgmRig rg[3];
@@ -243,14 +245,15 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
             char *b = c->modevols.as<char>() + (size_t)(k - 1) * per;
             a.cost = reinterpret_cast<uint16_t *>(b);
             a.sum0 = reinterpret_cast<uint16_t *>(b + vol);
-            a.sum1 = reinterpret_cast<uint16_t *>(b + 2 * vol);
-            a.bnd = reinterpret_cast<uint16_t *>(b + 3 * vol);
-            a.progress = reinterpret_cast<unsigned *>(b + 3 * vol + bnd);
+            a.sum1 = reinterpret_cast<uint16_t *>(b + vol + svol);
+            a.bnd = reinterpret_cast<uint16_t *>(b + vol + 2 * svol);
+            a.progress = reinterpret_cast<unsigned *>(b + vol + 2 * svol + bnd);
         }
         a.W = g.Wp;
         a.H = g.Hp;
         a.D = g.dc;
         a.nbands = plan.nbands;
+        if (cropped) sgm_crop_window(a, g);
     }
     const int nitems = 2 * plan.nbands * nm;
     const size_t rig_bytes = 3 * sizeof(SgmRig), item_off = (rig_bytes + 255) & ~(size_t)255;
@@ -293,13 +296,14 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
     c->mark(SISTER_STAGE_AGGREGATE);
     for (int k = 0; k < nm; k++) {
         e = launch_sgm_wta(g, rg[k].sum0, rg[k].sum1, dev_out[modes[k]],
-                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)modes[k] * g.plane : nullptr, st);
+                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)modes[k] * g.plane : nullptr, st, cropped);
         if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
     }
     c->mark(SISTER_STAGE_WTA);
     c->last_mode = modes[nm - 1];
     c->last_cost = rg[nm - 1].cost;
     c->last_sum0 = rg[nm - 1].sum0;
+    c->last_cropped = cropped;
     c->have_intermediates = true;
     return SISTER_OK;
 }
@@ -348,16 +352,19 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
         a.sum1 = c->sum1.as<uint16_t>();
         a.bnd = c->bnd.as<uint16_t>();
         a.progress = c->progress.as<unsigned>();
+        const bool cropped = !c->full_disp; // the pass sums of the original image only, unless the padded map is kept
+        if (cropped) sgm_crop_window(a, g);
         e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st, c->wait_limit_us);
         if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
         c->mark(SISTER_STAGE_AGGREGATE);
         e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode],
-                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)mode * g.plane : nullptr, st);
+                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)mode * g.plane : nullptr, st, cropped);
         if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
         c->mark(SISTER_STAGE_WTA);
         c->last_mode = mode;
         c->last_cost = a.cost;
         c->last_sum0 = a.sum0;
+        c->last_cropped = cropped;
     }
     c->have_intermediates = true;
     return SISTER_OK;
@@ -535,7 +542,7 @@ int sister_stereo(sister_ctx *c, const uint8_t *center, const uint8_t *other, in
     if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
     // WTALeft / WTARight (hpp:141-142) into maps 0 and 1 of frame 0, their in-place medians (hpp:143-144), LR check
     uint16_t *wta = c->wta.as<uint16_t>();
-    e = launch_sgm_wta(g, a.sum0, a.sum1, nullptr, wta, st);
+    e = launch_sgm_wta(g, a.sum0, a.sum1, nullptr, wta, st, false); // the whole plane: WTARight reads its diagonals
     if (e == cudaSuccess) e = launch_sgm_wta_right(g, a.sum0, a.sum1, wta + plane, st);
     if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
     launch_median(wta, g, c->med.as<uint16_t>(), st, 0, 1);
@@ -584,9 +591,10 @@ size_t sister_device_bytes(int width, int height, int dc) {
     if (p.R < 1) p = sgm_plan_gb300(g);
     if (p.R < 1) return 0;
     const size_t nbands = (size_t)p.nbands;
-    const size_t bnd = 2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2;
-    return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + 3 * vol * 2 +
-           bnd + sgm_progress_bytes(2 * nbands) + 3 * plane * 2 + 3 * (size_t)width * height * 2;
+    const size_t bnd = sgm_bnd_bytes(g, p);
+    // one compute of one mode without the padded map: the cost volume and two pass sums of the original image
+    return 5 * (size_t)width * height + 8 * plane + 8 * plane * 8 + 2 * 8 * plane * 2 + 4 * plane + vol * 2 +
+           2 * sgm_sum_cells(g, true) * 2 + bnd + sgm_progress_bytes(2 * nbands) + 2 + 3 * (size_t)width * height * 2;
 }
 
 int sister_profile_enable(sister_ctx *c, int on) {
@@ -674,7 +682,12 @@ int sister_debug_fetch(sister_ctx *c, int what, int index, void *dst, size_t byt
     case SISTER_DBG_MEDIAN: src = c->med.as<char>() + (size_t)index * plane * 2; need = plane * 2; break;
     case SISTER_DBG_MASKS: src = c->masks.as<char>() + (size_t)index * plane; need = plane; break;
     case SISTER_DBG_COST: src = reinterpret_cast<const char *>(c->last_cost); need = plane * g.dp * 2; break;
-    case SISTER_DBG_SUM0: src = reinterpret_cast<const char *>(c->last_sum0); need = plane * g.dp * 2; break;
+    case SISTER_DBG_SUM0:
+        if (c->last_cropped)
+            return c->fail(SISTER_ESTATE, "the whole pass-0 sum volume is kept only with SISTER_TUNE_FULL_DISP = 1");
+        src = reinterpret_cast<const char *>(c->last_sum0);
+        need = plane * g.dp * 2;
+        break;
     case SISTER_DBG_DISP:
         if (!c->full_disp) return c->fail(SISTER_ESTATE, "the padded disparity map is kept only with SISTER_TUNE_FULL_DISP = 1");
         src = c->disp.as<char>() + (size_t)index * plane * 2;

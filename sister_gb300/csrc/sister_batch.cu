@@ -32,8 +32,8 @@ constexpr size_t kStagingBytes = 4u << 20; // pinned staging for item lists and 
 
 size_t al(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
-// Device bytes of one rig inside a wave: prep buffers shared by its modes, plus per mode the cost and the
-// two pass sums, the band hand-off records, progress counters and the output image.
+// Device bytes of one rig inside a wave: prep buffers shared by its modes, plus per mode the cost, the two pass
+// sums of the original image's pixels, the band hand-off records, progress counters and the output image.
 struct RigBytes {
     size_t prep = 0, per_mode = 0;
 };
@@ -45,8 +45,8 @@ RigBytes rig_bytes(int w, int h, int dc, int channels, int R) {
              al(8 * plane * 8) + 2 * al(8 * plane * 2) + al(4 * plane) +
              al(4 * (size_t)std::max(g.Wp, g.Hp) * sizeof(unsigned)); // pair WTA row flags
     const size_t nbands = (size_t)(g.Hp + R - 1) / R;
-    const size_t vol = plane * g.dp * 2;
-    b.per_mode = 3 * al(vol) + al(2 * nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2) + al(progress_bytes(2 * nbands)) +
+    const size_t vol = plane * g.dp * 2, svol = sgm_sum_cells(g, true) * 2;
+    b.per_mode = al(vol) + 2 * al(svol) + al(sgm_bnd_bytes(g, SgmPlan{})) + al(progress_bytes(2 * nbands)) +
                  al((size_t)w * h * 2);
     return b;
 }
@@ -170,11 +170,11 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
             j.mode = mode;
             j.g = g;
             j.nbands = (g.Hp + R - 1) / R;
-            const size_t vol = plane * g.dp * 2;
+            const size_t vol = plane * g.dp * 2, svol = sgm_sum_cells(g, true) * 2;
             j.cost = b->take<uint16_t>(vol);
-            j.sum0 = b->take<uint16_t>(vol);
-            j.sum1 = b->take<uint16_t>(vol);
-            j.bnd = b->take<uint16_t>(2 * (size_t)j.nbands * g.Wp * (3 * (size_t)g.dp + 8) * 2);
+            j.sum0 = b->take<uint16_t>(svol);
+            j.sum1 = b->take<uint16_t>(svol);
+            j.bnd = b->take<uint16_t>(sgm_bnd_bytes(g, SgmPlan{}));
             j.progress = b->take<unsigned>(progress_bytes(2 * (size_t)j.nbands));
             j.out = b->take<uint16_t>((size_t)w * h * 2);
             j.host_out = outs[mode];
@@ -229,6 +229,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
                 rg.H = j.g.Hp;
                 rg.D = j.g.dc;
                 rg.nbands = j.nbands;
+                sgm_crop_window(rg, j.g); // no padded map: the sums of the original image only
             }
             std::copy(items.begin(), items.end(), hi);
             SgmRig *dr = b->take<SgmRig>(rig_bytes_n);
@@ -246,7 +247,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
     // every final WTA first, then the copies: a copy into pageable host memory returns only once it is done, so
     // interleaving them would leave the GPU idle between WTAs
     for (const Job &j : jobs) {
-        e = launch_sgm_wta(j.g, j.sum0, j.sum1, j.out, nullptr, b->main);
+        e = launch_sgm_wta(j.g, j.sum0, j.sum1, j.out, nullptr, b->main, true);
         if (e != cudaSuccess) return b->cuda_fail(e, "winner-take-all");
     }
     for (const Job &j : jobs) {

@@ -66,8 +66,8 @@ Layout layout(const Geom &g, int channels, int nmodes, const SgmPlan &p) {
     L.med = take(8 * plane * 2);
     L.masks = take(4 * plane);
     L.cost = take(vol);
-    L.sum0 = take(vol);
-    L.sum1 = take(vol);
+    L.sum0 = take(sgm_sum_cells(g, true) * 2); // the pass sums of the original image only (no padded map)
+    L.sum1 = take(sgm_sum_cells(g, true) * 2);
     L.bnd = take(sgm_bnd_bytes(g, p));
     L.progress = take(sgm_progress_bytes(std::max(p.ngroups, 1)));
     L.outs = take((size_t)nmodes * img * 2);
@@ -459,8 +459,9 @@ int Engine::enqueue(Job *j, std::string *err) {
         a.sum1 = reinterpret_cast<uint16_t *>(b + L.sum1);
         a.bnd = reinterpret_cast<uint16_t *>(b + L.bnd);
         a.progress = reinterpret_cast<unsigned *>(b + L.progress);
+        sgm_crop_window(a, g);
         e = launch_sgm(g, j->plan, a, errflag, st, wait_limit_us_);
-        if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, dout, nullptr, st);
+        if (e == cudaSuccess) e = launch_sgm_wta(g, a.sum0, a.sum1, dout, nullptr, st, true);
         uint16_t *hdst = j->stage_out ? reinterpret_cast<uint16_t *>(static_cast<char *>(pinned_[j->slot].p) + kAlign +
                                                                      (j->stage_in ? al(5 * img * ch) : 0)) +
                                             (size_t)k * img

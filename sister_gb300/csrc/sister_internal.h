@@ -46,14 +46,27 @@ constexpr unsigned kDrainLimitUs = 2000000;
 // One rig's aggregation buffers (all device pointers).
 struct SgmRig {
     const uint16_t *cost; // [Hp][Wp][dp] masked multiview cost
-    uint16_t *sum0;       // [Hp][Wp][dp] 4-path sum of pass 0 (top-down)
-    uint16_t *sum1;       // [Hp][Wp][dp] 4-path sum of pass 1 (bottom-up)
-    uint16_t *bnd;        // [2][nbands][Wp][3dp+8] r1/r2/r3 states + minima of each band's last row, per pass
+    uint16_t *sum0;       // [sh][sw][dp] 4-path sum of pass 0 (top-down) over the stored window
+    uint16_t *sum1;       // [sh][sw][dp] 4-path sum of pass 1 (bottom-up) over the stored window
+    uint16_t *bnd;        // [2][2][Wp][3dp+8] r1/r2/r3 states + minima of a band's last row: pass, band parity
     unsigned *progress;   // [2][nbands] x kProgressStride: pixels of a band's last row published so far, per
                           // pass, one counter per 128-byte line (zeroed first)
     int W, H, D;          // padded width and height, max disparity dc
     int nbands;           // bands per pass = ceil(H / R)
+    // Window of padded pixels whose sums are stored: columns [sx0, sx0 + sw), rows [sy0, sy0 + sh). sw = 0 stores
+    // the whole padded plane; sgm_crop_window keeps only the original image (the only pixels the final WTA reads
+    // when no padded map is asked for).
+    int sx0, sy0, sw, sh;
 };
+// Store only the original image's pixels (padded offset dc) of the pass sums: volumes of w*h*dp cells.
+inline void sgm_crop_window(SgmRig &r, const Geom &g) {
+    r.sx0 = g.dc;
+    r.sy0 = g.dc;
+    r.sw = g.w;
+    r.sh = g.h;
+}
+// cells of one pass-sum volume: the original image with a cropped window, else the padded plane
+inline size_t sgm_sum_cells(const Geom &g, bool cropped) { return (cropped ? (size_t)g.w * g.h : g.plane) * g.dp; }
 
 // Arguments of one aggregation launch: the work items of one or several rigs that share the d-stride dp
 // (same kernel instantiation) and the band height R.
@@ -106,6 +119,8 @@ void launch_masked_cost(const uint64_t *census, const uint8_t *masks, const Geom
 // force_R: 0 = choose automatically; force_cs is accepted and ignored (groups are single bands)
 SgmPlan sgm_plan(const Geom &g, int device, int force_R = 0, int force_cs = 0);
 SgmPlan sgm_plan_gb300(const Geom &g); // the plan on a 152-SM GB300, without a device query
+// band hand-off records of one rig: two rows of Wp records per pass, reused by every other band (independent of
+// the plan)
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
 // single rig: rig.nbands is filled from the plan; rig.progress (sgm_progress_bytes(p.ngroups): the counters and
 // the item ticket) is zeroed here
@@ -122,8 +137,9 @@ cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,
                                  cudaStream_t st);
-// disp (padded Hp x Wp map) may be null: then only the cropped output pixels are computed
+// disp (padded Hp x Wp map) may be null: then only the cropped output pixels are computed. cropped: the sums hold
+// only the original image's pixels (sgm_crop_window; disp must then be null)
 cudaError_t launch_sgm_wta(const Geom &g, const uint16_t *sum0, const uint16_t *sum1, uint16_t *out, uint16_t *disp,
-                           cudaStream_t st);
+                           cudaStream_t st, bool cropped);
 
 } // namespace sister

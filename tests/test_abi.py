@@ -56,8 +56,8 @@ def test_device_bytes_estimate(lib):
     small = lib.sister_device_bytes(640, 480, 192)
     big = lib.sister_device_bytes(1920, 1080, 256)
     assert 0 < small < big
-    # the aggregation volumes dominate: two u16 volumes of (w+2dc)(h+2dc)dc
-    assert big >= 2 * 2 * 2432 * 1592 * 256
+    # the aggregation volumes dominate: the u16 cost volume of (w+2dc)(h+2dc)dc and two pass sums of w*h*dc
+    assert big >= 2 * (2432 * 1592 + 2 * 1920 * 1080) * 256
     assert lib.sister_device_bytes(0, 480, 192) == 0
 
 

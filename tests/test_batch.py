@@ -102,9 +102,10 @@ def test_batch_waves_under_a_small_budget(gpu_lib):
 
 def test_batch_rejects_oversized_rig_and_bad_geometry(gpu_lib):
     views, _ = synth.make_rig(160, 120, 4, 40, seed=5, tiles=4)
-    b = sg.Batch(0, 32 << 20)
+    need = sg.Batch.rig_bytes(160, 120, 64, 1)
+    b = sg.Batch(0, need // 2)
     with pytest.raises(sg.SisterError) as ei:
-        b.run([(views, 64)])  # ~44 MB for one mode
+        b.run([(views, 64)])  # twice the budget for one mode
     assert ei.value.code == sg.SISTER_EBUDGET
     with pytest.raises(sg.SisterError) as ei:
         b.run([(views, 60)])  # not a multiple of 8

@@ -41,6 +41,9 @@ def test_stress_rig_4096x3000_dc512(gpu_lib):
     bad = disp != want_d
     assert not bad.any(), "%d px differ from the fixture (first at %s)" % (int(bad.sum()), np.argwhere(bad)[0])
     assert out_sha(multi) == str(z["multi_sha"])
+    # the same rig without the padded map: pass sums stored for the original image only
+    ctx.tune_set(sg.TUNE_FULL_DISP, 0)
+    assert out_sha(ctx.compute(True, False, False)[0]) == str(z["multi_sha"])
     disp = disp.astype(np.int64)
     # output encoding: 255 * d saturated to 65535
     assert np.array_equal(multi.astype(np.int64), np.minimum(disp * 255, 65535))
