@@ -36,17 +36,22 @@ CONFIG = {
     "workload": "plain single rig: 5 views 1920x1080 u8, maxdisp 256, multiview output (mode 0)",
     "w": W_, "h": H_, "dc": DC, "seed": SEED,
     "generator": "seeded synthetic scene: 16 planar tiles + quadratic bump, disparity 10-240 px",
-    "l2": "L2 flushed (256 MB write) before every timed step; cost and sum volumes (2 x 2 GB) exceed L2",
+    "l2": "L2 flushed (256 MB write) before every timed step; the cost volume (2 GB) and pass sums (2 x 1 GB) exceed L2",
     "parallelism": "replicas (one rig per GPU per step, no collective)",
 }
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 # kernels of ours launched per compute: frames, census, pair WTA + medians (one launch), masks, cost,
-# aggregation (both passes), final WTA
-KERNELS_PER_COMPUTE = 7
-# DRAM bytes per padded cell of one aggregation launch, measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on a 480x320 rig at max disparity 256: 0.817 + 1.110 GB for 992*832*256 cells. It exceeds
-# the 8 algorithmic bytes per cell by the band hand-off records; scaled to other rigs by the cell count.
-TRAFFIC_BYTES_PER_CELL = (0.816880640e9 + 1.109881e9) / (992 * 832 * 256)
+# aggregation (both passes and the final WTA of every output row, one launch)
+KERNELS_PER_COMPUTE = 6
+# DRAM bytes of one aggregation launch (both passes and the fused final WTA): the u16 cost volume read by both passes
+# (4 B per padded cell) and the two pass sums of the output pixels written and read back by the WTA rows (8 B per
+# output cell), times the ratio ncu measured on the 1920x1080/256 launch itself (dram__bytes_read.sum +
+# dram__bytes_write.sum = 6.07 + 2.41 GB against the model's 3.965 + 4.246 GB).
+TRAFFIC_CAL = (6.07e9 + 2.41e9) / (4 * 2432 * 1592 * 256 + 8 * 1920 * 1080 * 256)
+
+
+def agg_traffic(w: int, h: int, dc: int) -> float:
+    return TRAFFIC_CAL * (4.0 * (w + 2 * dc) * (h + 2 * dc) * dc + 8.0 * w * h * dc)
 # integer operations of the algorithm per padded cell: masked 4-pair cost (popcounts, masks, selects, adds) ~36,
 # 8 aggregation paths x 8 (3 minima, saturating adds and subtraction, running minimum), the 8-path sum 7, pair WTA
 # (left and right) 8, final WTA 2 -- about 98 -- and the 32-bit popcounts among them: 8 for the cost and 8 for the
@@ -554,9 +559,10 @@ def run_gb300(args):
                   "ms_per_call": ms3, "value": rig_units() / (ms3 / 1e3), "unit": UNIT + " (w*h*dc per call)",
                   "outputs_per_s_value": 3 * rig_units() / (ms3 / 1e3), "bit_exact_vs_reference_golden": ok3}
 
-    # roofline of the dominant kernel (the aggregation launch, both passes), with the algorithmic bytes of the
-    # algorithm's aggregation: the u16 sum volume written once and read once, 4 B per padded cell (the launch's
-    # own traffic -- both passes read the cost volume and write their own sum -- is reported as `traffic`)
+    # roofline of the dominant kernel (the aggregation launch: both passes and the final WTA), with the algorithmic
+    # bytes of the algorithm's aggregation: the u16 sum volume written once and read once, 4 B per padded cell (the
+    # launch's own traffic -- both passes read the cost volume, the output pixels' sums are written and read back --
+    # is reported as `traffic`)
     cells = (w + 2 * dc) * (h + 2 * dc) * dc
     sgm = stage_ms.get("aggregate", [])
     peak, peak_kind = load_peaks()
@@ -565,11 +571,12 @@ def run_gb300(args):
     if sgm:
         avg = sum(sgm) / len(sgm)
         achieved = 4.0 * cells / (avg / 1e3) / 1e9
-        roof = {"kernel": "sgm_kernel (8-path aggregation, both passes in one launch)", "bound": "hbm",
+        roof = {"kernel": "sgm_kernel (8-path aggregation, both passes and the final WTA in one launch)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": TRAFFIC_BYTES_PER_CELL * cells,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of sgm_kernel<8> on a 480x320/256 "
-                                  "rig (1.93 GB for 211 M padded cells), scaled to this launch by the cell count",
+                "traffic": agg_traffic(w, h, dc),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of sgm_kernel<8> on the "
+                                  "1920x1080/256 launch (6.07 + 2.41 GB: the cost volume read by both passes, the "
+                                  "output pixels' pass sums written and read back), modelled for other rigs",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": 4 * cells, "launch_ms": avg}
     # whole step against the integer roofline: 98 integer ops per padded cell (the algorithm's count), against the

@@ -45,6 +45,7 @@
 #include "tuned_gb300.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 namespace sister {
@@ -293,6 +294,35 @@ __device__ __forceinline__ uint32_t path_step(const uint32_t (&P)[NP], uint32_t 
     return hmin2(mn);
 }
 
+// ---------------------------------------------------------------- final winner-take-all of one pixel
+// The lowest d <= min(j, D-1) of S0 + S1 at padded column j (postprocess.cpp:74-185), one warp per pixel, this
+// lane holding d = d0 .. d0 + 2 NP - 1: keys (sum << 16) | d; halves with d >= D or d > j are forced to sum 0xFFFF
+// (real sums are smaller, and both halves of a pair are real or both infinite since dc % 8 == 0). Pixels with
+// j >= dp-1 in a volume whose stride holds only real disparities (D = dp) need neither test (warp-uniform).
+template <int NP>
+__device__ __forceinline__ uint32_t wta_pixel(const uint32_t (&s0)[NP], const uint32_t (&s1)[NP], int d0, int j, int D,
+                                              int dp) {
+    uint32_t best = 0xFFFFFFFFu;
+    if (j >= dp - 1 && D == dp) {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const int d = d0 + 2 * k;
+            const uint32_t sv = s0[k] + s1[k];
+            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const int d = d0 + 2 * k;
+            uint32_t sv = s0[k] + s1[k];
+            if (d >= D || d > j) sv |= 0x0000FFFFu;
+            if (d + 1 >= D || d + 1 > j) sv |= 0xFFFF0000u;
+            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
+        }
+    }
+    return __reduce_min_sync(FULL, best) & 0xFFFFu;
+}
+
 // ---------------------------------------------------------------- the kernel
 template <int DPL>
 __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_kernel(const SgmLaunch a) {
@@ -346,20 +376,78 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
         __syncthreads();
         const int item = *s_item;
         if (item >= a.nitems) break;
-        int band;
+        int band, wrow = -1; // a band item (pass, band) or a final-WTA item (cropped row wrow)
         SgmRig rg;
         if (a.items) {
             const uint32_t v = a.items[item];
             rg = a.rigs[v >> 24];
-            band = (int)((v >> 1) & 0x7FFFFFu);
+            band = (int)((v >> 1) & kItemIndexMask);
             pass = (int)(v & 1u);
+            if (v & kItemWta) wrow = band;
         } else {
             rg = a.rig0;
             band = item >> 1;
             pass = item & 1;
+            if (item >= 2 * rg.nbands) wrow = sgm_wta_row(item - 2 * rg.nbands, rg.sh);
         }
         W = rg.W;
         H = rg.H;
+        if (wrow >= 0) {
+            // ===================================================== final WTA of one cropped row (fused)
+            // Both passes' bands holding padded row i have published their sums (a band item releases its flag
+            // after the CTA barrier that ends it); every band item was drawn before any WTA item, so the wait ends.
+            const int i = rg.sy0 + wrow;
+            if (threadIdx.x == 0) {
+                const unsigned *f0 = rg.progress + ((size_t)(i / R)) * kProgressStride + 1;
+                const unsigned *f1 = rg.progress + ((size_t)rg.nbands + (H - 1 - i) / R) * kProgressStride + 1;
+                const unsigned long long t0 = global_ns();
+                for (unsigned n = 0; ld_acquire(f0) == 0u || ld_acquire(f1) == 0u; n++) {
+                    __nanosleep(256);
+                    if (n % kCheckEvery == kCheckEvery - 1 &&
+                        (ld_relaxed(a.err) != kErrNone || global_ns() - t0 > 1000ull * a.wait_limit_us)) {
+                        atomicCAS(a.err, kErrNone, kErrTimeout);
+                        break;
+                    }
+                }
+            }
+            __syncthreads();
+            constexpr int U = 4; // pixels of one warp in flight
+            const int nwarps = blockDim.x >> 5;
+            const size_t rowcell = (size_t)wrow * rg.sw;
+            for (int x0 = wi * U; x0 < rg.sw; x0 += nwarps * U) {
+                uint32_t s0[U][NP], s1[U][NP];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int x = min(x0 + u, rg.sw - 1);
+                    const uint4 *p0 = reinterpret_cast<const uint4 *>(rg.sum0 + (rowcell + x) * dp + d0);
+                    const uint4 *p1 = reinterpret_cast<const uint4 *>(rg.sum1 + (rowcell + x) * dp + d0);
+                    if constexpr (NP % 4 == 0) {
+#pragma unroll
+                        for (int k = 0; k < NP / 4; k++) {
+                            const uint4 v0 = __ldcg(p0 + k), v1 = __ldcg(p1 + k);
+                            s0[u][4 * k] = v0.x; s0[u][4 * k + 1] = v0.y; s0[u][4 * k + 2] = v0.z; s0[u][4 * k + 3] = v0.w;
+                            s1[u][4 * k] = v1.x; s1[u][4 * k + 1] = v1.y; s1[u][4 * k + 2] = v1.z; s1[u][4 * k + 3] = v1.w;
+                        }
+                    } else {
+                        const unsigned *q0 = reinterpret_cast<const unsigned *>(p0), *q1 = reinterpret_cast<const unsigned *>(p1);
+#pragma unroll
+                        for (int k = 0; k < NP; k++) {
+                            s0[u][k] = __ldcg(q0 + k);
+                            s1[u][k] = __ldcg(q1 + k);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int x = x0 + u;
+                    if (x >= rg.sw) break; // warp-uniform
+                    const uint32_t dv = wta_pixel<NP>(s0[u], s1[u], d0, rg.sx0 + x, rg.D, dp);
+                    if (lane == 0) rg.out[rowcell + x] = (uint16_t)min(dv * 255u, 0xFFFFu);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
 #pragma unroll
         for (int k = 0; k < NP; k++)
             padm[k] = ((d0 + 2 * k < rg.D) ? 0u : 0x0000FFFFu) | ((d0 + 2 * k + 1 < rg.D) ? 0u : 0xFFFF0000u);
@@ -669,6 +757,11 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
             }
         }
         __syncthreads();
+        // a band item's sums are complete: release its flag for the fused WTA items of its rows
+        if (rg.out && threadIdx.x == 0) {
+            __threadfence();
+            st_release(progress + (size_t)band * kProgressStride + 1, 1u);
+        }
     }
 }
 
@@ -700,29 +793,8 @@ __global__ void __launch_bounds__(256) sgm_wta_kernel(const uint16_t *__restrict
     uint32_t s0[NP], s1[NP];
     ldw<NP>(s0v + cell * g.dp + d0, s0);
     ldw<NP>(s1v + cell * g.dp + d0, s1);
-    // keys (sum << 16) | d; halves with d >= dc or d > j are forced to sum 0xFFFF (real sums are smaller). Pixels
-    // with j >= dp-1 in a volume whose stride holds only real disparities (dc = dp) need neither test (warp-uniform)
-    uint32_t best = 0xFFFFFFFFu;
-    if (j >= g.dp - 1 && D == g.dp) {
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            const int d = d0 + 2 * k;
-            const uint32_t sv = s0[k] + s1[k];
-            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            const int d = d0 + 2 * k;
-            uint32_t sv = s0[k] + s1[k]; // both halves of a pair are real or both infinite (dc % 8 == 0)
-            if (d >= D || d > j) sv |= 0x0000FFFFu;
-            if (d + 1 >= D || d + 1 > j) sv |= 0xFFFF0000u;
-            best = min(best, min(__byte_perm(sv, (uint32_t)d, 0x1054), __byte_perm(sv, (uint32_t)(d + 1), 0x3254)));
-        }
-    }
-    best = __reduce_min_sync(FULL, best);
+    const uint32_t dv = wta_pixel<NP>(s0, s1, d0, j, D, g.dp);
     if (lane == 0) {
-        const uint32_t dv = best & 0xFFFFu;
         if (disp) disp[pix] = (uint16_t)dv;
         const int oi = i - g.dc, oj = j - g.dc;
         if (out && oi >= 0 && oi < g.h && oj >= 0 && oj < g.w) out[(size_t)oi * g.w + oj] = (uint16_t)min(dv * 255u, 0xFFFFu);
@@ -900,7 +972,8 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
     a.rig0 = rig;
     a.rigs = nullptr;
     a.items = nullptr;
-    a.nitems = p.ngroups;
+    if (rig.out && rig.sw == 0) return cudaErrorInvalidValue; // the fused WTA reads sums of the original image
+    a.nitems = p.ngroups + (rig.out ? rig.sh : 0);
     a.R = p.R;
     a.dp = g.dp;
     a.claim = rig.progress + (size_t)p.ngroups * kProgressStride;
@@ -912,6 +985,38 @@ cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *er
     // each work item depends only on items drawn before it (the previous band of its pass), so a plain launch
     // of any grid size completes
     return cudaLaunchKernel(fn, dim3(p.nclusters), dim3((p.R + kHelpers) * 32), args, sgm_smem(p.R, g.dp).total, st);
+}
+
+void sgm_build_items(const SgmItemRig *rigs, int nrigs, int R, bool fuse, std::vector<uint32_t> &items) {
+    items.clear();
+    int maxb = 0;
+    for (int k = 0; k < nrigs; k++) maxb = std::max(maxb, rigs[k].nbands);
+    // position of band item (rig k, pass, band) in the band order: first[k][band] + pass
+    std::vector<std::vector<int>> first(nrigs);
+    for (int k = 0; k < nrigs; k++) first[k].assign(rigs[k].nbands, 0);
+    for (int band = 0; band < maxb; band++)
+        for (int k = 0; k < nrigs; k++)
+            if (band < rigs[k].nbands) {
+                first[k][band] = (int)items.size();
+                for (int pass = 0; pass < 2; pass++) items.push_back(sgm_item_band(k, band, pass));
+            }
+    if (!fuse) return;
+    struct W {
+        int key;  // position of the later of the row's two band items
+        int dist; // distance of the row from its rig's middle row (ties: nearest the middle first)
+        uint32_t item;
+    };
+    std::vector<W> ws;
+    for (int k = 0; k < nrigs; k++)
+        for (int c = 0; c < rigs[k].sh; c++) {
+            const int i = rigs[k].sy0 + c;
+            const int e = std::max(first[k][i / R], first[k][(rigs[k].H - 1 - i) / R] + 1);
+            ws.push_back({e, std::abs(2 * c + 1 - rigs[k].sh), sgm_item_wta(k, c)});
+        }
+    std::stable_sort(ws.begin(), ws.end(), [](const W &a, const W &b) {
+        return a.key != b.key ? a.key < b.key : a.dist < b.dist;
+    });
+    for (const W &w : ws) items.push_back(w.item);
 }
 
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,

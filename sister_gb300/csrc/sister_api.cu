@@ -213,10 +213,11 @@ int ensure_buffers(sister_ctx *c, const Geom &g) {
     return SISTER_OK;
 }
 
-// Several modes of one rig (the reference's compute_disparities computes all three, hpp:77-89): each mode's masked
-// cost into its own volume, then ONE aggregation launch over the work items of every mode (items ordered by
-// band, so each follows the previous band of its mode and pass), then each mode's final WTA. One launch instead of
-// one per mode: the wavefront ramp and tail of each mode are filled by the other modes' bands.
+// The requested modes of one rig (the reference's compute_disparities computes all three, hpp:77-89): each mode's
+// masked cost into its own volume, then ONE aggregation launch over the work items of every mode (band items
+// ordered by band, so each follows the previous band of its mode and pass; without the padded map each mode's
+// final WTA rows follow as work items of the same launch, see sgm_build_items). One launch instead of one per mode:
+// the wavefront ramp and tail of each mode are filled by the other modes' bands and by the WTA rows.
 int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16_t *dev_out[3]) {
     cudaStream_t st = c->stream;
     int modes[3], nm = 0, mask = 0;
@@ -226,6 +227,7 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
             mask |= 1 << m;
         }
     const bool cropped = !c->full_disp; // the pass sums of the original image only, unless the padded map is kept
+    const bool fuse = cropped && g.dp <= kFuseWtaMaxDp; // the final WTA as work items of the aggregation launch
     const size_t vol = g.plane * g.dp * sizeof(uint16_t), svol = sgm_sum_cells(g, cropped) * sizeof(uint16_t);
     const size_t bnd = sgm_bnd_bytes(g, plan), prog = sgm_progress_bytes(std::max(plan.ngroups, 1));
     const size_t per = vol + 2 * svol + bnd + prog; // cost, sum0, sum1, hand-off records, progress counters
@@ -254,8 +256,15 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
         a.D = g.dc;
         a.nbands = plan.nbands;
         if (cropped) sgm_crop_window(a, g);
+        if (fuse) a.out = dev_out[modes[k]];
     }
-    const int nitems = 2 * plan.nbands * nm;
+    std::vector<uint32_t> items;
+    {
+        const SgmItemRig ir{plan.nbands, g.Hp, g.dc, g.h};
+        const SgmItemRig irs[3] = {ir, ir, ir};
+        sgm_build_items(irs, nm, plan.R, fuse, items);
+    }
+    const int nitems = (int)items.size();
     const size_t rig_bytes = 3 * sizeof(SgmRig), item_off = (rig_bytes + 255) & ~(size_t)255;
     const size_t claim_off = (item_off + (size_t)nitems * 4 + 255) & ~(size_t)255;
     e = c->desc.ensure(claim_off + progress_bytes(1));
@@ -263,11 +272,6 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
     char *desc = c->desc.as<char>();
     if (c->desc_key[0] != g.w || c->desc_key[1] != g.h || c->desc_key[2] != g.dc || c->desc_key[3] != mask ||
         std::memcmp(c->desc_rigs, rg, (size_t)nm * sizeof(SgmRig)) != 0) {
-        std::vector<uint32_t> items;
-        items.reserve(nitems);
-        for (int band = 0; band < plan.nbands; band++)
-            for (int k = 0; k < nm; k++)
-                for (uint32_t pass = 0; pass < 2; pass++) items.push_back((uint32_t)k << 24 | (uint32_t)band << 1 | pass);
         e = cudaMemcpyAsync(desc, rg, rig_bytes, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(desc + item_off, items.data(), items.size() * 4, cudaMemcpyHostToDevice, st);
@@ -294,11 +298,12 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
                              c->wait_limit_us);
     if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
     c->mark(SISTER_STAGE_AGGREGATE);
-    for (int k = 0; k < nm; k++) {
-        e = launch_sgm_wta(g, rg[k].sum0, rg[k].sum1, dev_out[modes[k]],
-                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)modes[k] * g.plane : nullptr, st, cropped);
-        if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
-    }
+    if (!fuse)
+        for (int k = 0; k < nm; k++) {
+            e = launch_sgm_wta(g, rg[k].sum0, rg[k].sum1, dev_out[modes[k]],
+                               cropped ? nullptr : c->disp.as<uint16_t>() + (size_t)modes[k] * g.plane, st, cropped);
+            if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
+        }
     c->mark(SISTER_STAGE_WTA);
     c->last_mode = modes[nm - 1];
     c->last_cost = rg[nm - 1].cost;
@@ -341,33 +346,12 @@ int run_pipeline(sister_ctx *c, uint16_t *dev_out[3]) {
     if (e != cudaSuccess) return c->cuda_fail(e, "mask stage launch");
     const SgmPlan &plan = plan_for(c, g);
     const int nmodes = (dev_out[0] ? 1 : 0) + (dev_out[1] ? 1 : 0) + (dev_out[2] ? 1 : 0);
-    if (nmodes > 1) return run_modes_together(c, g, plan, dev_out);
-    for (int mode = 0; mode < 3; mode++) {
-        if (!dev_out[mode]) continue;
-        launch_masked_cost(c->census.as<uint64_t>(), c->masks.as<uint8_t>(), g, mode, c->cost.as<uint16_t>(), st);
-        c->mark(SISTER_STAGE_COST);
-        SgmRig a{};
-        a.cost = c->cost.as<uint16_t>();
-        a.sum0 = c->sum0.as<uint16_t>();
-        a.sum1 = c->sum1.as<uint16_t>();
-        a.bnd = c->bnd.as<uint16_t>();
-        a.progress = c->progress.as<unsigned>();
-        const bool cropped = !c->full_disp; // the pass sums of the original image only, unless the padded map is kept
-        if (cropped) sgm_crop_window(a, g);
-        e = launch_sgm(g, plan, a, c->errflag.as<unsigned>(), st, c->wait_limit_us);
-        if (e != cudaSuccess) return c->cuda_fail(e, "aggregation launch");
-        c->mark(SISTER_STAGE_AGGREGATE);
-        e = launch_sgm_wta(g, a.sum0, a.sum1, dev_out[mode],
-                           c->full_disp ? c->disp.as<uint16_t>() + (size_t)mode * g.plane : nullptr, st, cropped);
-        if (e != cudaSuccess) return c->cuda_fail(e, "winner-take-all launch");
-        c->mark(SISTER_STAGE_WTA);
-        c->last_mode = mode;
-        c->last_cost = a.cost;
-        c->last_sum0 = a.sum0;
-        c->last_cropped = cropped;
+    if (nmodes == 0) { // nothing to aggregate: the mask-stage intermediates are still available for inspection
+        c->have_intermediates = true;
+        return SISTER_OK;
     }
-    c->have_intermediates = true;
-    return SISTER_OK;
+    // one aggregation launch for every requested output (each mode's cost into its own volume)
+    return run_modes_together(c, g, plan, dev_out);
 }
 
 int read_device_error(sister_ctx *c) {

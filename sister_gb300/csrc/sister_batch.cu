@@ -202,15 +202,12 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
         const int R = sgm_rows_max(dp, b->device);
         for (size_t c0 = 0; c0 < cls.size(); c0 += 256) {
             const size_t c1 = std::min(cls.size(), c0 + 256);
-            // items ordered by band: every item follows the previous band of its job and pass
-            int maxb = 0;
-            for (size_t q = c0; q < c1; q++) maxb = std::max(maxb, cls[q]->nbands);
+            // items ordered by band: every item follows the previous band of its job and pass; every job's final
+            // WTA rows are placed after the bands that complete them (sgm_build_items)
+            std::vector<SgmItemRig> irs;
+            for (size_t q = c0; q < c1; q++) irs.push_back({cls[q]->nbands, cls[q]->g.Hp, cls[q]->g.dc, cls[q]->g.h});
             std::vector<uint32_t> items;
-            for (int band = 0; band < maxb; band++)
-                for (size_t q = c0; q < c1; q++)
-                    if (band < cls[q]->nbands)
-                        for (uint32_t pass = 0; pass < 2; pass++)
-                            items.push_back((uint32_t)(q - c0) << 24 | (uint32_t)band << 1 | pass);
+            sgm_build_items(irs.data(), (int)irs.size(), R, dp <= kFuseWtaMaxDp, items);
             const size_t rig_bytes_n = (c1 - c0) * sizeof(SgmRig), item_bytes = items.size() * sizeof(uint32_t);
             if (soff + al(rig_bytes_n) + al(item_bytes) > kStagingBytes)
                 return b->fail(SISTER_EBUDGET, "batch wave has too many aggregation work items (%zu)", items.size());
@@ -230,6 +227,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
                 rg.D = j.g.dc;
                 rg.nbands = j.nbands;
                 sgm_crop_window(rg, j.g); // no padded map: the sums of the original image only
+                if (dp <= kFuseWtaMaxDp) rg.out = j.out; // the final WTA runs in the same launch
             }
             std::copy(items.begin(), items.end(), hi);
             SgmRig *dr = b->take<SgmRig>(rig_bytes_n);
@@ -244,12 +242,12 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
             if (e != cudaSuccess) return b->cuda_fail(e, "aggregation launch");
         }
     }
-    // every final WTA first, then the copies: a copy into pageable host memory returns only once it is done, so
-    // interleaving them would leave the GPU idle between WTAs
-    for (const Job &j : jobs) {
-        e = launch_sgm_wta(j.g, j.sum0, j.sum1, j.out, nullptr, b->main, true);
-        if (e != cudaSuccess) return b->cuda_fail(e, "winner-take-all");
-    }
+    // the final WTA of the jobs whose launch does not take it (wide d-strides), then the copies
+    for (const Job &j : jobs)
+        if (j.g.dp > kFuseWtaMaxDp) {
+            e = launch_sgm_wta(j.g, j.sum0, j.sum1, j.out, nullptr, b->main, true);
+            if (e != cudaSuccess) return b->cuda_fail(e, "winner-take-all");
+        }
     for (const Job &j : jobs) {
         const sister_rig &r = rigs[j.rig];
         e = cudaMemcpyAsync(j.host_out, j.out, (size_t)r.width * r.height * 2, cudaMemcpyDeviceToHost, b->main);

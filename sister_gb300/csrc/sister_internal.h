@@ -5,6 +5,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace sister {
 
 // Geometry of one rig (reference naming: width/height are the padded frame sizes of doMultiStereo,
@@ -57,6 +59,9 @@ struct SgmRig {
     // the whole padded plane; sgm_crop_window keeps only the original image (the only pixels the final WTA reads
     // when no padded map is asked for).
     int sx0, sy0, sw, sh;
+    // [sh][sw] disparity*255 (saturated): when set (with a cropped window), the launch also runs the final WTA of
+    // every output row as work items after the band items; else the sums are left for launch_sgm_wta
+    uint16_t *out;
 };
 // Store only the original image's pixels (padded offset dc) of the pass sums: volumes of w*h*dp cells.
 inline void sgm_crop_window(SgmRig &r, const Geom &g) {
@@ -67,6 +72,17 @@ inline void sgm_crop_window(SgmRig &r, const Geom &g) {
 }
 // cells of one pass-sum volume: the original image with a cropped window, else the padded plane
 inline size_t sgm_sum_cells(const Geom &g, bool cropped) { return (cropped ? (size_t)g.w * g.h : g.plane) * g.dp; }
+
+// Work items of a multi-rig aggregation launch: rig << 24 | kind | index << 1 | pass. A band item (index = band)
+// aggregates R rows of one pass; a fused final-WTA item (kind kItemWta, index = a row of the original image) takes
+// the winner-take-all of one output row once both passes' bands holding it are done. All band items of a launch
+// come before its WTA items.
+constexpr uint32_t kItemWta = 1u << 23, kItemIndexMask = (1u << 22) - 1u;
+inline uint32_t sgm_item_band(int rig, int band, int pass) { return (uint32_t)rig << 24 | (uint32_t)band << 1 | (uint32_t)pass; }
+inline uint32_t sgm_item_wta(int rig, int row) { return (uint32_t)rig << 24 | kItemWta | (uint32_t)row << 1; }
+// The j-th output row in WTA item order: the rows nearest the middle of the image first (both passes finish the
+// middle bands first), then alternately one above and one below.
+__host__ __device__ inline int sgm_wta_row(int j, int h) { return h / 2 + ((j & 1) ? -((j + 1) >> 1) : (j >> 1)); }
 
 // Arguments of one aggregation launch: the work items of one or several rigs that share the d-stride dp
 // (same kernel instantiation) and the band height R.
@@ -123,7 +139,7 @@ SgmPlan sgm_plan_gb300(const Geom &g); // the plan on a 152-SM GB300, without a 
 // the plan)
 size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &p);
 // single rig: rig.nbands is filled from the plan; rig.progress (sgm_progress_bytes(p.ngroups): the counters and
-// the item ticket) is zeroed here
+// the item ticket) is zeroed here; with rig.out set the launch also takes the final WTA (rig.sh more items)
 cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
                        unsigned wait_limit_us = kDefaultWaitUs);
 // several rigs of one d-stride class: rigs / items in device memory (progress counters and the item ticket
@@ -133,6 +149,20 @@ int sgm_rows_gb300(int dp); // sgm_rows_max on a GB300, without a device query
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
                              unsigned *claim, unsigned *err, int device, cudaStream_t st,
                              unsigned wait_limit_us = kDefaultWaitUs);
+// Work items of a multi-rig launch. Band items are ordered by band (then rig, then pass), so every item follows the
+// previous band of its rig and pass. With `fuse`, every rig's output rows (rows sy0 .. sy0+sh-1 of its padded
+// plane) follow all band items as final-WTA items, in the order in which their two bands come in the band order
+// (nearest the middle first among equals). Spreading them among the band items instead (each one grid of items
+// after its bands) measured slower: a CTA drawn away from the bands lengthens the wavefront's critical path.
+// rigs: {nbands, H, sy0, sh}.
+struct SgmItemRig {
+    int nbands, H, sy0, sh;
+};
+void sgm_build_items(const SgmItemRig *rigs, int nrigs, int R, bool fuse, std::vector<uint32_t> &items);
+// The final WTA joins the aggregation launch for d-strides up to this (measured faster at 1920x1080/256 one and
+// three outputs, 640x480/192 and the uneven batch; at 4096x3000/512 the separate kernel is faster: the 25 GB of
+// pass sums gather in the launch's tail)
+constexpr int kFuseWtaMaxDp = 256;
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,
