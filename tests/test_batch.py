@@ -91,6 +91,22 @@ def test_batch_benchmark_shapes_match_oracle(gpu_lib, port):
         assert np.array_equal(g[0], want), "shape %s: %d px differ" % (shapes[pick[k]], int((g[0] != want).sum()))
 
 
+def test_batch_wide_strides_match_oracle(gpu_lib, port):
+    """d-strides above 256 (final WTA as a separate kernel) batched with narrower ones (final WTA inside the
+    aggregation launch), against the oracle."""
+    specs = [(200, 120, 4, 240, 264), (160, 96, 2, 56, 64), (128, 96, 4, 290, 312), (96, 64, 2, 20, 24)]
+    rigs = []
+    for k, (w, h, lo, hi, dc) in enumerate(specs):
+        views, _ = synth.make_rig(w, h, lo, hi, seed=800 + k, tiles=4)
+        rigs.append((views, dc))
+    b = sg.Batch(0, 0)
+    got = b.run(rigs)
+    b.close()
+    for k, ((views, dc), g) in enumerate(zip(rigs, got)):
+        want = port.compute(views, dc, modes=(True, False, False))[0]
+        assert np.array_equal(g[0], want), "rig %d (dc %d): %d px differ" % (k, dc, int((g[0] != want).sum()))
+
+
 def test_batch_waves_under_a_small_budget(gpu_lib):
     rigs = _rigs(seed0=70)
     want = [_single(r) for r in rigs]

@@ -81,6 +81,20 @@ def test_requests_overlap_and_match_alone(gpu_lib):
     srv.close()
 
 
+def test_wide_stride_requests_match_oracle(gpu_lib, port):
+    """Requests whose d-stride is above 256 take the final WTA as a separate kernel (narrower ones inside the
+    aggregation launch); both kinds in one server, against the oracle."""
+    shapes = [(200, 120, 264), (160, 96, 64), (128, 96, 312)]
+    rigs = [_rig(k, shapes, seed0=700) for k in range(len(shapes))]
+    srv = sg.Server(0, 4 << 30)
+    tickets = [srv.submit(v, dc) for v, dc in rigs]
+    for k, t in enumerate(tickets):
+        out, _ = srv.wait(t)
+        want = port.compute(rigs[k][0], rigs[k][1], modes=(True, False, False))[0]
+        assert np.array_equal(out[0], want), "request %d: %d px differ" % (k, int((out[0] != want).sum()))
+    srv.close()
+
+
 def test_full_queue_refuses_and_pending_wait(gpu_lib):
     views, dc = _rig(0, [(640, 480, 128)], seed0=77)
     want = _single(views, dc)[0]
