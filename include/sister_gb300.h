@@ -135,8 +135,10 @@ enum {
     SISTER_TUNE_SGM_CLUSTER = 2,  /* CTAs per thread-block cluster (1, 2, 4 or 8); 0 = automatic */
     SISTER_TUNE_SGM_GROUPS = 3,   /* read-only: cluster-sized row groups of the current geometry */
     SISTER_TUNE_SGM_CLUSTERS = 4, /* read-only: co-resident clusters launched */
-    SISTER_TUNE_FULL_DISP = 5,    /* 1: also write the padded winner-take-all map (SISTER_DBG_DISP); 0 (default):
-                                     only the cropped outputs are computed */
+    SISTER_TUNE_FULL_DISP = 5,    /* 1: also write the padded winner-take-all map (SISTER_DBG_DISP) and keep the pass
+                                     sums of the whole padded plane (SISTER_DBG_SUM0), with the final WTA as its own
+                                     kernel; 0 (default): only the cropped outputs, pass sums of the original pixels,
+                                     the final WTA inside the aggregation launch */
     SISTER_TUNE_WAIT_LIMIT_US = 6 /* longest device-side wait of one warp on another warp or CTA (band hand-offs,
                                      median row flags) before the kernel gives up, raises its error flag and
                                      finishes: the compute then returns SISTER_ETIMEOUT and the context stays
@@ -215,7 +217,8 @@ enum {
     SISTER_DBG_MEDIAN = 4, /* index 2f / 2f+1: after the in-place median (u16) */
     SISTER_DBG_MASKS = 5,  /* index f: confidence mask of frame f in padded original coordinates (u8) */
     SISTER_DBG_COST = 6,   /* index 0: masked multiview cost of the last aggregated mode (u16, d stride dp) */
-    SISTER_DBG_SUM0 = 7,   /* index 0: pass-0 SGM sum of the last aggregated mode (u16, d stride dp) */
+    SISTER_DBG_SUM0 = 7,   /* index 0: pass-0 SGM sum of the last aggregated mode (u16, Hp x Wp x dp); needs
+                              SISTER_TUNE_FULL_DISP = 1 (otherwise only the original pixels' sums are kept) */
     SISTER_DBG_DISP = 8,   /* index mode: padded winner-take-all disparity (u16, Hp x Wp); needs SISTER_TUNE_FULL_DISP = 1 */
     SISTER_DBG_DP = 9      /* returns the padded disparity stride dp of the volumes in *(int*)dst */
 };
