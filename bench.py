@@ -292,7 +292,7 @@ def batched_leg(local):
             "engine": "continuous admission, 8 rigs in flight, one stream each"}
 
 
-def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 2000.0), seconds=2.0,
+def served_leg(local, rates=(25.0, 50.0, 100.0, 150.0, 200.0, 500.0, 1000.0, 2000.0), seconds=4.0,
                max_queue=32, max_inflight=8):
     """C4: Poisson arrivals of single-rig requests (mix: 50% 640x480/128, 35% 1920x1080/256, 15% 2448x2048/256)
     into the serving loop with a 16 GB device budget and continuous admission; requests beyond a queue of
