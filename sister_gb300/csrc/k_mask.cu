@@ -175,7 +175,7 @@ __device__ __forceinline__ uint32_t pmed3(uint32_t a, uint32_t b, uint32_t c) {
 // (high half of a, low half of b): the column pair shifted by one position
 __device__ __forceinline__ uint32_t shift1(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
 __device__ __forceinline__ uint32_t med3s(uint32_t a, uint32_t b, uint32_t c) { return max(min(a, b), min(max(a, b), c)); }
-constexpr int kMedPairs = 2; // packed position pairs per thread
+constexpr int kMedPairsMax = 2; // packed position pairs per thread in a pass over a chunk (1 or 2, per map)
 
 // median3x3_SSE(a, a, W, H) in place (postprocess.cpp:15-71 as called at SisterMultiviewDisparities.hpp:198
 // and siblings). Over the flattened array of N = W*H: out[x] = in[x] for x < W and x >= N-W-4;
@@ -196,6 +196,7 @@ constexpr int kMedPairs = 2; // packed position pairs per thread
 // read (the head, each chunk's staging, the tail) warp 0 waits until they are published with this epoch,
 // and a CTA barrier passes that on. The wait is bounded: on expiry the error flag is raised and the sweep goes on.
 constexpr int kMedPF = 3;
+template <int kMedPairs>
 __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, const Geom &g, uint16_t *__restrict__ med,
                                            int k, const unsigned *rowflags, unsigned epoch, unsigned *err,
                                            uint16_t *msm) {
@@ -331,11 +332,24 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
     for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
 }
 
+// One pair per thread where the block covers a chunk's pairs in one pass (a shorter chain per chunk: the pair WTA +
+// median stage of 640x480/192 0.565 -> 0.525 ms, of 640x480/128 0.44 -> 0.41 ms), else two (1920x1080/256's
+// transposed maps: one pass of two pairs beats two passes of one).
+__device__ __forceinline__ void median_map_any(const uint16_t *__restrict__ wta, const Geom &g, uint16_t *__restrict__ med,
+                                               int k, const unsigned *rowflags, unsigned epoch, unsigned *err,
+                                               uint16_t *msm) {
+    const int W = g.fcols(k >> 1);
+    if ((W - 1) / 2 <= (int)blockDim.x - 2)
+        median_map<1>(wta, g, med, k, rowflags, epoch, err, msm);
+    else
+        median_map<kMedPairsMax>(wta, g, med, k, rowflags, epoch, err, msm);
+}
+
 __global__ void __launch_bounds__(1024) median_kernel(const uint16_t *__restrict__ wta, Geom g,
                                                       uint16_t *__restrict__ med, int k0, const unsigned *rowflags,
                                                       unsigned epoch, unsigned *err) {
     extern __shared__ __align__(16) uint16_t msm[];
-    median_map(wta, g, med, k0 + blockIdx.x, rowflags, epoch, err, msm);
+    median_map_any(wta, g, med, k0 + blockIdx.x, rowflags, epoch, err, msm);
 }
 
 // Both WTAs of every frame row and the eight medians in one launch: blocks 0..7 sweep the medians of maps
@@ -349,7 +363,7 @@ __global__ void __launch_bounds__(1024) wta_median_kernel(const uint64_t *__rest
                                                           unsigned *rowflags, unsigned epoch, unsigned *err) {
     extern __shared__ __align__(16) uint64_t fsm[];
     if (blockIdx.x < 8) {
-        median_map(wta, g, med, blockIdx.x, rowflags, epoch, err, reinterpret_cast<uint16_t *>(fsm));
+        median_map_any(wta, g, med, blockIdx.x, rowflags, epoch, err, reinterpret_cast<uint16_t *>(fsm));
         return;
     }
     // row t of the merged sequence: A = rows of frames 1 and 3 (2 Wp), B = rows of frames 0 and 2 (2 Hp)
@@ -443,8 +457,8 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
                    const unsigned *rowflags, unsigned epoch, unsigned *err) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
-    // one thread per kMedPairs position pairs of a chunk (W-1 positions), plus one for the odd ends
-    int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
+    // one thread per position pair of a chunk (W-1 positions), plus one for the odd ends, up to 1024
+    int threads = ((mx - 1) / 2 + 2 + 31) & ~31;
     threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
     median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err);
 }
@@ -456,10 +470,10 @@ void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uin
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     // One block size for both kinds of block. The pair WTA rows run best at two blocks per SM (512 threads at its
     // 61 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM); a median
-    // block needs one thread per kMedPairs position pairs of a chunk to sweep a chunk in one pass, and 512 threads
-    // take the longest chunks of frames up to 4096 columns in at most two passes, which their shorter chains absorb.
-    int threads = (((mx - 1) / 2 + kMedPairs - 1) / kMedPairs + 1 + 31) & ~31;
-    threads = threads < 256 ? 256 : mx <= 4096 ? (threads > 512 ? 512 : threads) : (threads > 1024 ? 1024 : threads);
+    // block sweeps a chunk with one or two position pairs per thread (median_map_any), and 512 threads take the
+    // longest chunks of frames up to 4096 columns in at most two passes, which their shorter chains absorb.
+    int threads = ((mx - 1) / 2 / kMedPairsMax + 2 + 31) & ~31;
+    threads = mx <= 4096 ? 512 : (threads < 512 ? 512 : threads > 1024 ? 1024 : threads);
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
                                                                                        epoch, err);
