@@ -1,23 +1,11 @@
 // Confidence-mask kernels: per-pair WTA-left/right from census words, the reference's in-place
 // (row-recursive) 3x3 median, LR check and the per-pair masks in padded original coordinates.
 #include "sister_internal.h"
+#include "ptx_sync.h"
 
 namespace sister {
 namespace {
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
+using namespace ptx;
 
 // WTALeft_SSE / WTARight_SSE with uniqueness 1 (postprocess.cpp:74-315) on a pair's Hamming volume
 // (census.cpp:54-146), without materialising the volume. Both reduce to the lowest-index argmin of the
@@ -154,7 +142,7 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
-            st_release_u32(rowflags + (size_t)f * max(g.Wp, g.Hp) + i, epoch);
+            st_release(rowflags + (size_t)f * max(g.Wp, g.Hp) + i, epoch);
         }
     }
 }
@@ -174,7 +162,6 @@ __device__ __forceinline__ uint32_t pmed3(uint32_t a, uint32_t b, uint32_t c) {
 }
 // (high half of a, low half of b): the column pair shifted by one position
 __device__ __forceinline__ uint32_t shift1(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x5432); }
-__device__ __forceinline__ uint32_t med3s(uint32_t a, uint32_t b, uint32_t c) { return max(min(a, b), min(max(a, b), c)); }
 constexpr int kMedPairsMax = 2; // packed position pairs per thread in a pass over a chunk (1 or 2, per map)
 
 // median3x3_SSE(a, a, W, H) in place (postprocess.cpp:15-71 as called at SisterMultiviewDisparities.hpp:198
@@ -188,10 +175,11 @@ constexpr int kMedPairsMax = 2; // packed position pairs per thread in a pass ov
 // Inside a chunk the positions are taken in even-aligned pairs, two per 32-bit word: window column c of
 // position x is (out[c-W], in[c], in[c+W]); each packed column word is sorted once (packed min, median, max)
 // and the median of nine is med3(max of the column minima, med3 of the column medians, min of the column
-// maxima), the shifted columns coming from byte permutes of neighbouring words. A pair never straddles the
-// chunk end (position e depends on the chunk's first position), so an odd first position and an odd last one
-// are done one at a time. Halves of loaded words outside the chunk's columns only feed positions that are not
-// computed; they hold map values too (shared memory is zeroed first), so they cannot carry into a used half.
+// maxima), the shifted columns coming from byte permutes of neighbouring words. An odd first position s is the
+// high half of the pair (s-1, s) and an odd last one e-1 the low half of (e-1, e): only that half is stored (s-1
+// belongs to the previous chunk, and e depends on the chunk's first position), so every thread of a chunk runs
+// the same packed code. Halves of loaded words outside the chunk's columns only feed halves that are not stored;
+// they hold map values too (shared memory is zeroed first), so they cannot carry into a stored half.
 // With rowflags the kernel may run while the frame's pair WTA is still writing the map: before input rows are
 // read (the head, each chunk's staging, the tail) warp 0 waits until they are published with this epoch,
 // and a CTA barrier passes that on. The wait is bounded: on expiry the error flag is raised and the sweep goes on.
@@ -214,15 +202,18 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
     for (int o = threadIdx.x; o < (rlen + (kMedPF + 1) * blen) / 2; o += blockDim.x) reinterpret_cast<uint32_t *>(msm)[o] = 0u;
     const unsigned *flags = rowflags ? rowflags + (size_t)f * max(g.Wp, g.Hp) : nullptr;
     int ready = 0; // (warp 0) input rows known to be published
-    // warp 0 reads 32 consecutive row flags per poll and advances past the leading published ones
-    auto wait_rows = [&](int last) {
-        if (!flags || threadIdx.x >= 32) return;
+    // warp 0, until the rows holding positions up to idx are published: it reads 32 consecutive row flags per poll
+    // and advances past the leading published ones. While the rows are known published the call costs a compare
+    // (no division by W in the sweep: at 640x480/192 the pair WTA + median stage 0.52 -> 0.47 ms). Reading the
+    // next flags ahead with relaxed loads and a fence measured slower.
+    auto wait_upto = [&](int idx) {
+        if (!flags || threadIdx.x >= 32 || idx < ready * W) return;
         const int lane = threadIdx.x;
-        last = min(last, H - 1);
+        const int last = min(idx / W, H - 1);
         const unsigned long long t0 = global_ns();
         for (unsigned n = 1; ready <= last; n++) {
             const int r = ready + lane;
-            const unsigned ok = __ballot_sync(0xFFFFFFFFu, r >= H || ld_acquire_u32(flags + r) == epoch);
+            const unsigned ok = __ballot_sync(0xFFFFFFFFu, r >= H || ld_acquire(flags + r) == epoch);
             ready += (ok == 0xFFFFFFFFu) ? 32 : __ffs(~ok) - 1;
             if (ready > last) break;
             __nanosleep(100);
@@ -237,7 +228,7 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
             }
         }
     };
-    wait_rows(0);
+    wait_upto(0);
     __syncthreads();
     // head: x < W unchanged, x == W -> 0
     for (int x = threadIdx.x; x <= W; x += blockDim.x) {
@@ -247,20 +238,19 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
     }
     const int end = N - W - 4;
     const int per = W - 1;
-    // last input row a chunk starting at sc reads (its staged span ends below b1)
-    auto span_row = [&](int sc) { return (min(N, (min(sc + per, end) + W + 1 + 7) & ~7) - 1) / W; };
+    // end of the staged input span of the chunk starting at sc (N % 8 == 0)
+    auto span_end = [&](int sc) { return min(N, (min(sc + per, end) + W + 1 + 7) & ~7); };
     // chunk c covers [W+1 + c*per, min(+per, end)); its inputs span [s-1, e+W+1), staged from base(c)
     auto base = [&](int sc) { return (sc - 1) & ~7; };
     auto stage = [&](int sc, uint16_t *dst) {
         if (sc >= end) return;
-        const int ec = min(sc + per, end);
-        const int b0 = base(sc), b1 = min(N, (ec + W + 1 + 7) & ~7); // b1 <= N - 3 rounded up, N % 8 == 0
+        const int b0 = base(sc), b1 = span_end(sc);
         for (int o = threadIdx.x * 8; b0 + o < b1; o += blockDim.x * 8)
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst + o)),
                          "l"(in + b0 + o)
                          : "memory");
     };
-    wait_rows(span_row(W + 1 + (kMedPF - 1) * per));
+    wait_upto(span_end(W + 1 + (kMedPF - 1) * per) - 1);
     __syncthreads();
     for (int c = 0; c < kMedPF; c++) {
         stage(W + 1 + c * per, bufs + (size_t)c * blen);
@@ -269,7 +259,7 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
     int c = 0;
     for (int s = W + 1; s < end; s += per, c++) {
         asm volatile("cp.async.wait_group %0;" ::"n"(kMedPF - 1) : "memory");
-        if (s + kMedPF * per < end) wait_rows(span_row(s + kMedPF * per));
+        if (s + kMedPF * per < end) wait_upto(span_end(s + kMedPF * per) - 1);
         // this chunk's inputs (every thread's copies) are in, the previous chunk's outputs are in the ring,
         // the buffer of chunk c-1 is free for chunk c+kMedPF and that chunk's input rows are published
         __syncthreads();
@@ -277,10 +267,12 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
         asm volatile("cp.async.commit_group;" ::: "memory");
         const int e = min(s + per, end);
         const uint16_t *bi = bufs + (size_t)(c % (kMedPF + 1)) * blen - base(s); // bi[x] = in[x] for the span
-        const int sp = s + (s & 1);      // first even position
-        const int np = (e - sp) >> 1;    // whole pairs in [sp, e)
-        for (int t = threadIdx.x; t * kMedPairs < np; t += blockDim.x) {
-            const int x0 = sp + 2 * kMedPairs * t;
+        // pairs (x, x+1) at even x cover [s, e): a first pair (s-1, s) when s is odd stores only s, a last pair
+        // (e-1, e) when e is odd stores only e-1 (the other half reads columns outside the chunk's inputs)
+        const int s0 = s & ~1;
+        const int npr = (e - s0 + 1) >> 1;
+        for (int t = threadIdx.x; t * kMedPairs < npr; t += blockDim.x) {
+            const int x0 = s0 + 2 * kMedPairs * t;
             // packed column words j = 0 .. kMedPairs+1 hold columns (x0 + 2j - 2, x0 + 2j - 1)
             uint32_t lo[kMedPairs + 2], mi[kMedPairs + 2], hi[kMedPairs + 2];
 #pragma unroll
@@ -296,50 +288,38 @@ __device__ __forceinline__ void median_map(const uint16_t *__restrict__ wta, con
 #pragma unroll
             for (int j = 0; j < kMedPairs; j++) {
                 const int x = x0 + 2 * j;
-                if (x >= sp + 2 * np) break;
+                if (x >= e) break;
                 const uint32_t l3 = __vimax3_u16x2(shift1(lo[j], lo[j + 1]), lo[j + 1], shift1(lo[j + 1], lo[j + 2]));
                 const uint32_t m3 = pmed3(shift1(mi[j], mi[j + 1]), mi[j + 1], shift1(mi[j + 1], mi[j + 2]));
                 const uint32_t h3 = __vimin3_u16x2(shift1(hi[j], hi[j + 1]), hi[j + 1], shift1(hi[j + 1], hi[j + 2]));
                 const uint32_t v = pmed3(l3, m3, h3);
-                *reinterpret_cast<uint32_t *>(ring + (x & mask)) = v;
-                *reinterpret_cast<uint32_t *>(out + x) = v;
-            }
-        }
-        // an odd first position and an odd last one, one at a time (columns x-1 .. x+1, none past e)
-        if (threadIdx.x == blockDim.x - 1) {
-            for (int q = 0; q < 2; q++) {
-                const int x = q == 0 ? ((s & 1) ? s : -1) : (((e - sp) & 1) ? e - 1 : -1);
-                if (x < 0) continue;
-                uint32_t l[3], m[3], h[3];
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const int cx = min(x - 1 + j, e);
-                    const uint32_t a0 = ring[(cx - W) & mask], a1 = bi[cx], a2 = bi[cx + W];
-                    l[j] = min(min(a0, a1), a2);
-                    h[j] = max(max(a0, a1), a2);
-                    m[j] = med3s(a0, a1, a2);
+                if (x >= s && x + 1 < e) {
+                    *reinterpret_cast<uint32_t *>(ring + (x & mask)) = v;
+                    *reinterpret_cast<uint32_t *>(out + x) = v;
+                } else {
+                    const int xs = x >= s ? x : x + 1;
+                    const uint16_t h = (uint16_t)(x >= s ? v : v >> 16);
+                    ring[xs & mask] = h;
+                    out[xs] = h;
                 }
-                const uint32_t v = med3s(max(l[0], max(l[1], l[2])), med3s(m[0], m[1], m[2]), min(h[0], min(h[1], h[2])));
-                ring[x & mask] = (uint16_t)v;
-                out[x] = (uint16_t)v;
             }
         }
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     // tail: x >= N-W-4 unchanged
-    wait_rows(H - 1);
+    wait_upto(N - 1);
     __syncthreads();
     for (int x = N - W - 4 + threadIdx.x; x < N; x += blockDim.x) out[x] = in[x];
 }
 
-// One pair per thread where the block covers a chunk's pairs in one pass (a shorter chain per chunk: the pair WTA +
-// median stage of 640x480/192 0.565 -> 0.525 ms, of 640x480/128 0.44 -> 0.41 ms), else two (1920x1080/256's
+// One pair per thread where the block covers a chunk's W/2 pairs in one pass (a shorter chain per chunk: the pair
+// WTA + median stage of 640x480/192 0.565 -> 0.525 ms, of 640x480/128 0.44 -> 0.41 ms), else two (1920x1080/256's
 // transposed maps: one pass of two pairs beats two passes of one).
 __device__ __forceinline__ void median_map_any(const uint16_t *__restrict__ wta, const Geom &g, uint16_t *__restrict__ med,
                                                int k, const unsigned *rowflags, unsigned epoch, unsigned *err,
                                                uint16_t *msm) {
     const int W = g.fcols(k >> 1);
-    if ((W - 1) / 2 <= (int)blockDim.x - 2)
+    if (W / 2 <= (int)blockDim.x)
         median_map<1>(wta, g, med, k, rowflags, epoch, err, msm);
     else
         median_map<kMedPairsMax>(wta, g, med, k, rowflags, epoch, err, msm);
@@ -457,8 +437,8 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
                    const unsigned *rowflags, unsigned epoch, unsigned *err) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
     const size_t smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
-    // one thread per position pair of a chunk (W-1 positions), plus one for the odd ends, up to 1024
-    int threads = ((mx - 1) / 2 + 2 + 31) & ~31;
+    // one thread per position pair of a chunk (W/2 pairs cover its W-1 positions), up to 1024
+    int threads = (mx / 2 + 31) & ~31;
     threads = threads < 64 ? 64 : threads > 1024 ? 1024 : threads;
     median_kernel<<<2 * nf, threads, smem, st>>>(wta, g, med, 2 * f0, rowflags, epoch, err);
 }
@@ -472,7 +452,7 @@ void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uin
     // 61 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM); a median
     // block sweeps a chunk with one or two position pairs per thread (median_map_any), and 512 threads take the
     // longest chunks of frames up to 4096 columns in at most two passes, which their shorter chains absorb.
-    int threads = ((mx - 1) / 2 / kMedPairsMax + 2 + 31) & ~31;
+    int threads = (mx / 2 / kMedPairsMax + 31) & ~31;
     threads = mx <= 4096 ? 512 : (threads < 512 ? 512 : threads > 1024 ? 1024 : threads);
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,

@@ -42,6 +42,7 @@
 // inside a pair whose sums are never read (the final minimum masks d >= dc).
 // Every wait is bounded: on expiry the device error flag is raised and the kernel finishes.
 #include "sister_internal.h"
+#include "ptx_sync.h"
 #include "tuned_gb300.h"
 
 #include <algorithm>
@@ -103,61 +104,7 @@ constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr uint32_t INF2 = 0x7FFF7FFFu;
 
 // ---------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t sptr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ void mbar_init(uint32_t a, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_inval(uint32_t a) {
-    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t a) {
-    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
-                 : "memory");
-}
-// 1D bulk copy global -> shared of this CTA, completion counted on mbarrier `bar`
-// (both addresses 16-byte aligned, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-// non-blocking test of the phase of parity `par`
-__device__ __forceinline__ bool mbar_test(uint32_t a, uint32_t par) {
-    uint32_t ok;
-    asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2; "
-                 "selp.u32 %0, 1, 0, p; }"
-                 : "=r"(ok)
-                 : "r"(a), "r"(par)
-                 : "memory");
-    return ok != 0;
-}
-// blocking test: the warp sleeps until the phase completes or about `ns` nanoseconds pass, so waiting
-// warps take no issue slots from the warps doing the arithmetic
-__device__ __forceinline__ bool mbar_sleep(uint32_t a, uint32_t par, uint32_t ns) {
-    uint32_t ok;
-    asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3; "
-                 "selp.u32 %0, 1, 0, p; }"
-                 : "=r"(ok)
-                 : "r"(a), "r"(par), "r"(ns)
-                 : "memory");
-    return ok != 0;
-}
+using namespace ptx;
 __device__ __forceinline__ void st_release_cta_shared(uint32_t a, unsigned v) {
     asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
@@ -166,12 +113,6 @@ __device__ __forceinline__ unsigned ld_acquire_cta_shared(uint32_t a) {
     asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
     return v;
 }
-__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-constexpr uint32_t kSleepNs = 20000; // suspend hint of one blocking test
 constexpr unsigned kCheckEvery = 64; // blocking tests between looks at the error flag and the clock (a
                                      // global load costs a memory round trip, which would delay every
                                      // hand-off that just missed its first test)
@@ -192,18 +133,6 @@ __device__ __forceinline__ void mbar_wait(uint32_t a, uint32_t par, const SgmLau
             }
         }
     }
-}
-// Wait for the phase of parity `par` with a time limit only (no early exit on the error flag): used to
-// drain bulk copies still in flight before barriers are re-initialised or the CTA exits.
-__device__ __forceinline__ void mbar_drain(uint32_t a, uint32_t par, unsigned limit_us) {
-    if (mbar_test(a, par)) return;
-    const unsigned long long t0 = global_ns();
-    while (!mbar_sleep(a, par, kSleepNs) && global_ns() - t0 <= 1000ull * limit_us) {
-    }
-}
-// order this thread's generic-proxy view of global memory (acquired records) before its bulk copies
-__device__ __forceinline__ void fence_proxy_async_global() {
-    asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
 // NP consecutive 32-bit words (2*NP u16) from / to shared or global memory, widest aligned accesses
@@ -475,8 +404,7 @@ __global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_k
                 for (int g = 0; g < 2; g++) mbar_init(cfull(wr, g), 1); // row warp's arrive.expect_tx + bytes
             for (int b = 0; b < NIB; b++) mbar_init(infull(b), 1);  // fetcher's arrive.expect_tx + bytes
             for (int x = 0; x < KI; x++) mbar_init(inempty(x), 32); // the first row's warp
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            fence_mbar_init();
         }
         first_band = false;
         __syncthreads();
