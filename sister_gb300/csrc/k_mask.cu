@@ -46,23 +46,37 @@ __device__ __forceinline__ uint32_t keypair(uint64_t xa, uint64_t xb, uint32_t d
 
 template <bool EDGE>
 __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64_t wB, int b0, int lane, int W,
-                                         int d0, int d1, uint32_t *lk, uint32_t *rk) {
+                                         int d0, int d1, uint32_t *lk, uint32_t *rk, uint32_t *done) {
     const int cA = b0 + 2 * lane, cB = cA + 1;
     uint32_t lacc = FULLW, racc = FULLW;
     // OR masks: a received U (V) counts for this lane's pair when lane >= 1 (2), else for an entering pair
     const uint32_t mU = lane >= 1 ? 0u : ~0u, mV = lane >= 2 ? 0u : ~0u;
+    // words cA+d and cA+d+1 of the next step: the previous step loaded them (two 16-byte loads per step; without
+    // EDGE the last step's second word may be the first of the neighbour row, in shared memory and never used)
+    uint64_t n0, n1;
+    if (EDGE) {
+        n0 = cc[min(cA + d0, W - 1)];
+        n1 = cc[min(cA + d0 + 1, W - 1)];
+    } else {
+        const ulonglong2 p = *reinterpret_cast<const ulonglong2 *>(cc + cA + d0);
+        n0 = p.x;
+        n1 = p.y;
+    }
 #pragma unroll 4
     for (int d = d0; d < d1; d += 4) {
-        uint64_t c[5];
+        uint64_t c[6];
+        c[0] = n0;
+        c[1] = n1;
         if (EDGE) {
 #pragma unroll
-            for (int t = 0; t < 5; t++) c[t] = cc[min(cA + d + t, W - 1)];
+            for (int t = 2; t < 6; t++) c[t] = cc[min(cA + d + t, W - 1)];
         } else {
-            const ulonglong2 p01 = *reinterpret_cast<const ulonglong2 *>(cc + cA + d);
             const ulonglong2 p23 = *reinterpret_cast<const ulonglong2 *>(cc + cA + d + 2);
-            c[0] = p01.x; c[1] = p01.y; c[2] = p23.x; c[3] = p23.y;
-            c[4] = cc[cA + d + 4];
+            const ulonglong2 p45 = *reinterpret_cast<const ulonglong2 *>(cc + cA + d + 4);
+            c[2] = p23.x; c[3] = p23.y; c[4] = p45.x; c[5] = p45.y;
         }
+        n0 = c[4];
+        n1 = c[5];
         uint32_t kab[4]; // (A_i, B_i)
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -80,12 +94,18 @@ __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64
         const uint32_t vr = __shfl_sync(FULLW, v, (lane + 30) & 31);
         lacc = __vminu2(__vimin3_u16x2(lacc, own, ur | mU), vr | mV);
         const uint32_t ent = __vminu2(ur | ~mU, vr | ~mV);
-        if (lane < 2) { // rows cA+d and cA+d+1 (< W: the unit's rows stay below b0 + dmax) are complete here
-            atomicMin(&lk[cA + d], lacc & 0xFFFFu);
-            atomicMin(&lk[cA + d + 1], lacc >> 16);
-        }
+        // rows cA+d and cA+d+1 (< W: the unit's rows stay below b0 + dmax) are complete here: lanes 0 and 1 hold rows
+        // b0+d .. b0+d+3, kept in the warp's buffer (word (d - d0)/2 + lane) and merged after the unit
+        if (lane < 2) done[((d - d0) >> 1) + lane] = lacc;
         lacc = __shfl_sync(FULLW, lane < 2 ? ent : lacc, (lane + 2) & 31);
     }
+    __syncwarp();
+    if (2 * lane < d1 - d0) { // rows b0+d0 .. b0+d1-1, two per lane
+        const uint32_t w = done[lane];
+        atomicMin(&lk[b0 + d0 + 2 * lane], w & 0xFFFFu);
+        atomicMin(&lk[b0 + d0 + 2 * lane + 1], w >> 16);
+    }
+    __syncwarp(); // the buffer is free for the warp's next unit
     // lane l now carries rows cA+d1 and cA+d1+1, which may have cells in other units
     if (cA + d1 < W && (lacc & 0xFFFFu) != 0xFFFFu) atomicMin(&lk[cA + d1], lacc & 0xFFFFu);
     if (cA + d1 + 1 < W && (lacc >> 16) != 0xFFFFu) atomicMin(&lk[cA + d1 + 1], lacc >> 16);
@@ -95,7 +115,7 @@ __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64
 
 // With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
 // i] = epoch (release), so that the frame's median can start on the first rows while later rows are computed.
-// Shared memory: both census rows (2 W words) and the L and R key arrays (2 W u32).
+// Shared memory: both census rows (2 W words), the L and R key arrays (2 W u32) and 32 u32 per warp.
 __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census, const Geom &g,
                                              uint16_t *__restrict__ wta, int f, int i, unsigned *rowflags,
                                              unsigned epoch, uint64_t *srow) {
@@ -120,6 +140,7 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
         }
         __syncthreads();
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        uint32_t *done = rk + W + 32 * warp; // the warp's completed rows of a unit
         const int nblk = (W + kWtaCols - 1) / kWtaCols, nch = (D + kWtaDiags - 1) / kWtaDiags;
         for (int u = warp; u < nblk * nch; u += nw) {
             const int blk = u / nch, ch = u - blk * nch;
@@ -129,8 +150,8 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
             if (d0 >= d1) continue; // warp-uniform
             const uint64_t wA = cn[min(b0 + 2 * lane, W - 1)], wB = cn[min(b0 + 2 * lane + 1, W - 1)];
             // the unit reads words up to cA + d1 (lane 31: b0 + 62 + d1)
-            if (b0 + kWtaCols - 2 + d1 < W) wta_unit<false>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk);
-            else wta_unit<true>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk);
+            if (b0 + kWtaCols - 2 + d1 < W) wta_unit<false>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk, done);
+            else wta_unit<true>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk, done);
         }
         __syncthreads();
         for (int j = threadIdx.x; j < W; j += blockDim.x) {
@@ -446,7 +467,7 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
                        unsigned epoch, unsigned *err, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t);
+    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t) + 32 * 32 * sizeof(uint32_t);
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     // One block size for both kinds of block. The pair WTA rows run best at two blocks per SM (512 threads at its
     // 61 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM); a median
