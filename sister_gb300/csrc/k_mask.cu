@@ -16,7 +16,7 @@ using namespace ptx;
 // lowest key is the lowest cost and, among equal costs, the lowest d, which is the reference's tie rule. Two keys
 // share each 32-bit word, so every packed minimum and every shuffle serves two cells.
 // Rows 0..2 (all 255) and rows H-2, H-1 (never written, defined 0) have constant costs: argmin 0.
-// One CTA per frame row; both census rows are staged in shared memory, and the row's band is cut into work
+// One CTA per frame row; the centre census row is staged in shared memory, and the row's band is cut into work
 // units of 64 columns x 64 diagonals spread over the CTA's warps.
 // In a unit, lane l holds the adjacent columns cA = b0+2l and cB = cA+1 and walks the diagonals four per step.
 // At step d it meets cells A_i = (cA+d+i, cA) and B_i = (cB+d+i, cB), i = 0..3: eight cells from the five words
@@ -52,7 +52,8 @@ __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64
     // OR masks: a received U (V) counts for this lane's pair when lane >= 1 (2), else for an entering pair
     const uint32_t mU = lane >= 1 ? 0u : ~0u, mV = lane >= 2 ? 0u : ~0u;
     // words cA+d and cA+d+1 of the next step: the previous step loaded them (two 16-byte loads per step; without
-    // EDGE the last step's second word may be the first of the neighbour row, in shared memory and never used)
+    // EDGE the last step's second word may be the first word after the row, the key array in shared memory, never
+    // used)
     uint64_t n0, n1;
     if (EDGE) {
         n0 = cc[min(cA + d0, W - 1)];
@@ -115,7 +116,8 @@ __device__ __forceinline__ void wta_unit(const uint64_t *cc, uint64_t wA, uint64
 
 // With rowflags, each block publishes its frame row when both maps' rows are written: rowflags[f * max(Wp, Hp) +
 // i] = epoch (release), so that the frame's median can start on the first rows while later rows are computed.
-// Shared memory: both census rows (2 W words), the L and R key arrays (2 W u32) and 32 u32 per warp.
+// Shared memory: the centre census row (W words), the L and R key arrays (2 W u32) and 32 u32 per warp; the
+// neighbour row's words are read from global memory, two per lane and work unit.
 __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census, const Geom &g,
                                              uint16_t *__restrict__ wta, int f, int i, unsigned *rowflags,
                                              unsigned epoch, uint64_t *srow) {
@@ -128,13 +130,12 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
             R[j] = 0;
         }
     } else {
-        uint64_t *cc = srow, *cn = srow + W;
-        uint32_t *lk = reinterpret_cast<uint32_t *>(srow + 2 * W), *rk = lk + W;
+        uint64_t *cc = srow;
+        uint32_t *lk = reinterpret_cast<uint32_t *>(srow + W), *rk = lk + W;
         const uint64_t *gc = census + (size_t)(2 * f) * g.plane + (size_t)i * W;
         const uint64_t *gn = census + (size_t)(2 * f + 1) * g.plane + (size_t)i * W;
         for (int j = threadIdx.x; j < W; j += blockDim.x) {
             cc[j] = gc[j];
-            cn[j] = gn[j];
             lk[j] = FULLW;
             rk[j] = FULLW;
         }
@@ -148,7 +149,8 @@ __device__ __forceinline__ void pair_wta_row(const uint64_t *__restrict__ census
             const int dmax = min(D, W - b0); // a multiple of 4 (D of 8, W of 4, b0 of 64)
             const int d0 = kWtaDiags * ch, d1 = min(d0 + kWtaDiags, dmax);
             if (d0 >= d1) continue; // warp-uniform
-            const uint64_t wA = cn[min(b0 + 2 * lane, W - 1)], wB = cn[min(b0 + 2 * lane + 1, W - 1)];
+            // the unit's two neighbour words per lane come straight from global memory (read-only here)
+            const uint64_t wA = __ldg(gn + min(b0 + 2 * lane, W - 1)), wB = __ldg(gn + min(b0 + 2 * lane + 1, W - 1));
             // the unit reads words up to cA + d1 (lane 31: b0 + 62 + d1)
             if (b0 + kWtaCols - 2 + d1 < W) wta_unit<false>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk, done);
             else wta_unit<true>(cc, wA, wB, b0, lane, W, d0, d1, lk, rk, done);
@@ -467,14 +469,15 @@ void launch_median(const uint16_t *wta, const Geom &g, uint16_t *med, cudaStream
 void launch_wta_median(const uint64_t *census, const Geom &g, uint16_t *wta, uint16_t *med, unsigned *rowflags,
                        unsigned epoch, unsigned *err, cudaStream_t st) {
     const int mx = g.Wp > g.Hp ? g.Wp : g.Hp;
-    const size_t pw_smem = 2 * (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t) + 32 * 32 * sizeof(uint32_t);
+    const size_t pw_smem = (size_t)mx * sizeof(uint64_t) + 2 * (size_t)mx * sizeof(uint32_t) + 32 * 32 * sizeof(uint32_t);
     const size_t md_smem = ((size_t)median_ring(mx) + (kMedPF + 1) * (2 * (size_t)mx + 32)) * sizeof(uint16_t);
     // One block size for both kinds of block. The pair WTA rows run best at two blocks per SM (512 threads at its
-    // 61 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM); a median
-    // block sweeps a chunk with one or two position pairs per thread (median_map_any), and 512 threads take the
-    // longest chunks of frames up to 4096 columns in at most two passes, which their shorter chains absorb.
-    int threads = (mx / 2 / kMedPairsMax + 31) & ~31;
-    threads = mx <= 4096 ? 512 : (threads < 512 ? 512 : threads > 1024 ? 1024 : threads);
+    // 53 registers: 1.67 ms for the rows of 1920x1080/256 against 1.93 at 640 threads, one block per SM; with the
+    // neighbour row read from global memory the blocks of 4096x3000/512 fit two per SM too: 17.9 -> 17.1 ms at 512
+    // threads against 1024); a median block sweeps a chunk with one or two position pairs per thread
+    // (median_map_any), in as many passes as the chunk needs (three for 5120 columns, faster than two at 1024
+    // threads: 4.9 against 5.3 ms for the eight medians of 4096x3000/512).
+    const int threads = 512;
     const unsigned blocks = 8u + 2u * (unsigned)g.Wp + 2u * (unsigned)g.Hp;
     wta_median_kernel<<<blocks, threads, pw_smem > md_smem ? pw_smem : md_smem, st>>>(census, g, wta, med, rowflags,
                                                                                        epoch, err);
