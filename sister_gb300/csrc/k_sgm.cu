@@ -56,14 +56,19 @@ constexpr int kKP = 4;      // ring slots of a row read by the row below
 constexpr int kKS = 8;      // ring slots of the band's last row, read by the writer
 constexpr int kBndRows = 2; // global hand-off rows per pass (a power of two), reused by every other band
 // most rows per band (one warp each) by d-stride; shared memory may allow fewer
-__host__ __device__ constexpr int rows_cap(int dp) { return dp <= 256 ? 14 : dp <= 384 ? 12 : 9; }
-// pixels per batched copy: cost group of a row, and records per fetch
-__host__ __device__ constexpr int batch_px(int dp) { return dp >= 384 ? 4 : 8; }
+__host__ __device__ constexpr int rows_cap(int dp) { return dp <= 256 ? 14 : 12; }
+// Pixels per batched copy (cost group of a row, and records per fetch) by d-stride and band height. At d-stride 512
+// bands above 9 rows fit in shared memory only with cost groups of 2 pixels; those run their own instantiation
+// (its launch bound for 12 row warps), which at 4096x3000/512 and 11 rows takes the aggregation from 32.5 to 30.5
+// ms, while smaller rigs of that d-stride stay fastest at 9 rows in groups of 4 (1280x960/512: 8.09 against 8.22).
+__host__ __device__ constexpr int batch_px(int dp, int R) { return dp >= 512 ? (R > 9 ? 2 : 4) : dp >= 384 ? 4 : 8; }
+// most rows per band of the instantiation with cost groups of FB pixels
+__host__ __device__ constexpr int rows_cap_fb(int dp, int FB) { return dp >= 512 && FB == 4 ? 9 : rows_cap(dp); }
 // pixels per hand-off batch between bands (batches of 2 measured fastest once the device-wide release moved off
 // the writer: 4.48 ms against 4.61 for 4 and 4.54 for 8 on 1920x1080/256), and the number of such batches the
 // incoming ring (2 * batch_px slots) holds, each with its own full barrier
 __host__ __device__ constexpr int hand_px(int) { return 2; }
-__host__ __device__ constexpr int in_batches(int dp) { return 2 * batch_px(dp) / hand_px(dp); }
+__host__ __device__ constexpr int in_batches(int dp, int R) { return 2 * batch_px(dp, R) / hand_px(dp); }
 
 // one pixel's record, in ring slots and in the global hand-off rows alike: r1 | r2 | r3 (dp u16 each) |
 // minima m1 m2 m3, each as a u32 pair (m, m) so that it feeds the packed arithmetic directly (+2 pad)
@@ -74,14 +79,14 @@ struct SgmSmem {
     int nbar, nslot;
 };
 // ring slots: row w < R-1 owns slots [w*kKP, w*kKP + kKP), row R-1 owns [(R-1)*kKP, (R-1)*kKP + kKS)
-// barriers (8 bytes each; FB = batch_px(dp), KI = 2*FB): slot k full at 2k, empty at 2k+1; then the incoming
+// barriers (8 bytes each; FB = batch_px(dp, R), KI = 2*FB): slot k full at 2k, empty at 2k+1; then the incoming
 // ring's batch full barriers [in_batches] and per-slot empty barriers [KI]; then cost group g (0, 1) of row w at
 // 2w + g
-__host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
+__host__ __device__ inline SgmSmem sgm_smem_fb(int R, int dp, int FB) {
     SgmSmem L{};
-    const int FB = batch_px(dp), KI = 2 * FB;
+    const int KI = 2 * FB;
     L.nslot = (R - 1) * kKP + kKS;
-    L.nbar = 2 * L.nslot + in_batches(dp) + KI + 2 * R;
+    L.nbar = 2 * L.nslot + KI / hand_px(dp) + KI + 2 * R;
     size_t o = 0;
     L.bars = o;
     o += (size_t)L.nbar * 8 + 16; // + the writer's count of records copied to global memory (u32) and the CTA's
@@ -97,6 +102,8 @@ __host__ __device__ inline SgmSmem sgm_smem(int R, int dp) {
     L.total = o;
     return L;
 }
+// the layout of a launch of band height R (its cost copies of batch_px(dp, R) pixels)
+__host__ __device__ inline SgmSmem sgm_smem(int R, int dp) { return sgm_smem_fb(R, dp, batch_px(dp, R)); }
 
 namespace {
 
@@ -253,20 +260,20 @@ __device__ __forceinline__ uint32_t wta_pixel(const uint32_t (&s0)[NP], const ui
 }
 
 // ---------------------------------------------------------------- the kernel
-template <int DPL>
-__global__ void __launch_bounds__((rows_cap(32 * DPL) + kHelpers) * 32, 1) sgm_kernel(const SgmLaunch a) {
+// FB: pixels per cost copy, batch_px(32 * DPL, a.R)
+template <int DPL, int FB>
+__global__ void __launch_bounds__((rows_cap_fb(32 * DPL, FB) + kHelpers) * 32, 1) sgm_kernel(const SgmLaunch a) {
     constexpr int NP = DPL / 2;
-    constexpr int FB = batch_px(32 * DPL); // pixels per cost copy
     constexpr int KI = 2 * FB;             // incoming-ring slots
     constexpr int HB = hand_px(32 * DPL);  // pixels per full hand-off batch
-    constexpr int NIB = in_batches(32 * DPL);
+    constexpr int NIB = 2 * FB / HB;       // in_batches(32 * DPL, a.R)
     extern __shared__ __align__(128) unsigned char smem[];
     const int R = a.R, dp = a.dp;
     int W = 0, H = 0; // geometry of the current work item's rig
     const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
     const int d0 = lane * DPL;
     const int rec = rec_u16(dp);
-    const SgmSmem L = sgm_smem(R, dp);
+    const SgmSmem L = sgm_smem_fb(R, dp, FB);
     const uint32_t bars = sptr(smem + L.bars);
     const uint32_t relcnt = bars + 8u * (uint32_t)L.nbar; // records of this band copied to global memory
     // ring of row w: kKP slots (kKS for the last row); slot k's full barrier at bars + 16k, empty at +8
@@ -754,14 +761,15 @@ __global__ void __launch_bounds__(256) sgm_wta_right_kernel(const uint16_t *__re
     if (lane == 0) disp[pix] = (uint16_t)(best & 0xFFFFu);
 }
 
-const void *kernel_for(int dpl) {
+// the instantiation for dpl disparities per lane and bands of R rows (R = 0: the one with the widest cost groups)
+const void *kernel_for(int dpl, int R) {
     switch (dpl) {
-    case 2: return (const void *)sgm_kernel<2>;
-    case 4: return (const void *)sgm_kernel<4>;
-    case 6: return (const void *)sgm_kernel<6>;
-    case 8: return (const void *)sgm_kernel<8>;
-    case 12: return (const void *)sgm_kernel<12>;
-    case 16: return (const void *)sgm_kernel<16>;
+    case 2: return (const void *)sgm_kernel<2, batch_px(64, 1)>;
+    case 4: return (const void *)sgm_kernel<4, batch_px(128, 1)>;
+    case 6: return (const void *)sgm_kernel<6, batch_px(192, 1)>;
+    case 8: return (const void *)sgm_kernel<8, batch_px(256, 1)>;
+    case 12: return (const void *)sgm_kernel<12, batch_px(384, 1)>;
+    case 16: return batch_px(512, R) == 2 ? (const void *)sgm_kernel<16, 2> : (const void *)sgm_kernel<16, 4>;
     default: return nullptr;
     }
 }
@@ -772,7 +780,9 @@ void init_sgm_kernels() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    for (int dpl : kDplChoices) cudaFuncSetAttribute(kernel_for(dpl), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    for (int dpl : kDplChoices)
+        for (int R : {1, rows_cap(32 * dpl)})
+            cudaFuncSetAttribute(kernel_for(dpl, R), cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaGetLastError();
     init_cost_kernels();
 }
@@ -847,8 +857,7 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaGetLastError();
-    const void *fn = kernel_for(g.dpl);
-    if (!fn) return SgmPlan{};
+    if (!kernel_for(g.dpl, 1)) return SgmPlan{};
     const int rmax = sgm_rows_max(g.dp, device);
     // on a 152-SM GB300, the band height the autotuner measured fastest for this geometry's class
     if (!force_R && sms == 152)
@@ -860,8 +869,8 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
     const int lo = force_R ? std::max(1, std::min(rmax, force_R)) : 1;
     return plan_rows(g, sms, lo, force_R ? lo : rmax, [&](int R) {
         int k = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, fn, (R + kHelpers) * 32, sgm_smem(R, g.dp).total) !=
-            cudaSuccess) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, kernel_for(g.dpl, R), (R + kHelpers) * 32,
+                                                          sgm_smem(R, g.dp).total) != cudaSuccess) {
             cudaGetLastError();
             k = 0;
         }
@@ -872,7 +881,7 @@ SgmPlan sgm_plan(const Geom &g, int device, int force_R, int /*force_cs: bands a
 // The same plan for a 152-SM GB300 without a device query (227 KB of shared memory per CTA, 228 KB and 64
 // warps per SM): used for memory estimates.
 SgmPlan sgm_plan_gb300(const Geom &g) {
-    if (!kernel_for(g.dpl)) return SgmPlan{};
+    if (!kernel_for(g.dpl, 1)) return SgmPlan{};
     return plan_rows(g, 152, 1, sgm_rows_gb300(g.dp), [&](int R) {
         return (int)std::min<size_t>(228 * 1024 / (sgm_smem(R, g.dp).total + 1024), 64 / (R + kHelpers));
     });
@@ -890,7 +899,7 @@ size_t sgm_bnd_bytes(const Geom &g, const SgmPlan &) {
 cudaError_t launch_sgm(const Geom &g, const SgmPlan &p, SgmRig rig, unsigned *err, cudaStream_t st,
                        unsigned wait_limit_us) {
     if (p.R < 1) return cudaErrorInvalidConfiguration;
-    const void *fn = kernel_for(g.dpl);
+    const void *fn = kernel_for(g.dpl, p.R);
     if (!fn) return cudaErrorInvalidValue;
     rig.W = g.Wp;
     rig.H = g.Hp;
@@ -950,7 +959,7 @@ void sgm_build_items(const SgmItemRig *rigs, int nrigs, int R, bool fuse, std::v
 cudaError_t launch_sgm_multi(int dp, int R, const SgmRig *rigs_dev, const uint32_t *items_dev, int nitems,
                              unsigned *claim, unsigned *err, int device, cudaStream_t st, unsigned wait_limit_us) {
     const int dpl = dp / 32;
-    const void *fn = kernel_for(dpl);
+    const void *fn = kernel_for(dpl, R);
     if (!fn || R < 1 || nitems < 1) return cudaErrorInvalidValue;
     int sms = 152, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
