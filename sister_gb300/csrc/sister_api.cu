@@ -227,7 +227,7 @@ int run_modes_together(sister_ctx *c, const Geom &g, const SgmPlan &plan, uint16
             mask |= 1 << m;
         }
     const bool cropped = !c->full_disp; // the pass sums of the original image only, unless the padded map is kept
-    const bool fuse = cropped && g.dp <= kFuseWtaMaxDp; // the final WTA as work items of the aggregation launch
+    const bool fuse = cropped; // the final WTA as work items of the aggregation launch (the padded map: its own kernel)
     const size_t vol = g.plane * g.dp * sizeof(uint16_t), svol = sgm_sum_cells(g, cropped) * sizeof(uint16_t);
     const size_t bnd = sgm_bnd_bytes(g, plan), prog = sgm_progress_bytes(std::max(plan.ngroups, 1));
     const size_t per = vol + 2 * svol + bnd + prog; // cost, sum0, sum1, hand-off records, progress counters

@@ -207,7 +207,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
             std::vector<SgmItemRig> irs;
             for (size_t q = c0; q < c1; q++) irs.push_back({cls[q]->nbands, cls[q]->g.Hp, cls[q]->g.dc, cls[q]->g.h});
             std::vector<uint32_t> items;
-            sgm_build_items(irs.data(), (int)irs.size(), R, dp <= kFuseWtaMaxDp, items);
+            sgm_build_items(irs.data(), (int)irs.size(), R, true, items);
             const size_t rig_bytes_n = (c1 - c0) * sizeof(SgmRig), item_bytes = items.size() * sizeof(uint32_t);
             if (soff + al(rig_bytes_n) + al(item_bytes) > kStagingBytes)
                 return b->fail(SISTER_EBUDGET, "batch wave has too many aggregation work items (%zu)", items.size());
@@ -227,7 +227,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
                 rg.D = j.g.dc;
                 rg.nbands = j.nbands;
                 sgm_crop_window(rg, j.g); // no padded map: the sums of the original image only
-                if (dp <= kFuseWtaMaxDp) rg.out = j.out; // the final WTA runs in the same launch
+                rg.out = j.out; // the final WTA runs in the same launch
             }
             std::copy(items.begin(), items.end(), hi);
             SgmRig *dr = b->take<SgmRig>(rig_bytes_n);
@@ -242,12 +242,7 @@ int run_wave(sister_batch *b, const sister_rig *rigs, int first, int last) {
             if (e != cudaSuccess) return b->cuda_fail(e, "aggregation launch");
         }
     }
-    // the final WTA of the jobs whose launch does not take it (wide d-strides), then the copies
-    for (const Job &j : jobs)
-        if (j.g.dp > kFuseWtaMaxDp) {
-            e = launch_sgm_wta(j.g, j.sum0, j.sum1, j.out, nullptr, b->main, true);
-            if (e != cudaSuccess) return b->cuda_fail(e, "winner-take-all");
-        }
+    // the outputs (every job's final WTA ran in its aggregation launch)
     for (const Job &j : jobs) {
         const sister_rig &r = rigs[j.rig];
         e = cudaMemcpyAsync(j.host_out, j.out, (size_t)r.width * r.height * 2, cudaMemcpyDeviceToHost, b->main);

@@ -460,9 +460,8 @@ int Engine::enqueue(Job *j, std::string *err) {
         a.bnd = reinterpret_cast<uint16_t *>(b + L.bnd);
         a.progress = reinterpret_cast<unsigned *>(b + L.progress);
         sgm_crop_window(a, g);
-        if (g.dp <= kFuseWtaMaxDp) a.out = dout; // the final WTA runs in the aggregation launch
+        a.out = dout; // the final WTA runs in the aggregation launch
         e = launch_sgm(g, j->plan, a, errflag, st, wait_limit_us_);
-        if (e == cudaSuccess && !a.out) e = launch_sgm_wta(g, a.sum0, a.sum1, dout, nullptr, st, true);
         uint16_t *hdst = j->stage_out ? reinterpret_cast<uint16_t *>(static_cast<char *>(pinned_[j->slot].p) + kAlign +
                                                                      (j->stage_in ? al(5 * img * ch) : 0)) +
                                             (size_t)k * img

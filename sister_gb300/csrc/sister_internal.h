@@ -159,10 +159,6 @@ struct SgmItemRig {
     int nbands, H, sy0, sh;
 };
 void sgm_build_items(const SgmItemRig *rigs, int nrigs, int R, bool fuse, std::vector<uint32_t> &items);
-// The final WTA joins the aggregation launch for d-strides up to this (measured faster at 1920x1080/256 one and
-// three outputs, 640x480/192 and the uneven batch; at 4096x3000/512 the separate kernel is faster: the 25 GB of
-// pass sums gather in the launch's tail)
-constexpr int kFuseWtaMaxDp = 256;
 // out: [h][w] disparity*255, disp: [Hp][Wp] padded disparity; either may be null
 // WTARight over S0 + S1 (two-view doStereo): lowest k <= min(dc-1, Wp-1-b) minimising S(i, b+k, k)
 cudaError_t launch_sgm_wta_right(const Geom &g, const uint16_t *s0, const uint16_t *s1, uint16_t *disp,

@@ -92,8 +92,8 @@ def test_batch_benchmark_shapes_match_oracle(gpu_lib, port):
 
 
 def test_batch_wide_strides_match_oracle(gpu_lib, port):
-    """d-strides above 256 (final WTA as a separate kernel) batched with narrower ones (final WTA inside the
-    aggregation launch), against the oracle."""
+    """d-strides above 256 (their own aggregation launches, with 12-row bands and 2-pixel cost copies at 512)
+    batched with narrower ones, against the oracle."""
     specs = [(200, 120, 4, 240, 264), (160, 96, 2, 56, 64), (128, 96, 4, 290, 312), (96, 64, 2, 20, 24)]
     rigs = []
     for k, (w, h, lo, hi, dc) in enumerate(specs):

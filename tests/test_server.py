@@ -82,8 +82,8 @@ def test_requests_overlap_and_match_alone(gpu_lib):
 
 
 def test_wide_stride_requests_match_oracle(gpu_lib, port):
-    """Requests whose d-stride is above 256 take the final WTA as a separate kernel (narrower ones inside the
-    aggregation launch); both kinds in one server, against the oracle."""
+    """Requests with d-strides above 256 (wider records and cost batches in the aggregation) beside a narrow one in
+    one server, against the oracle."""
     shapes = [(200, 120, 264), (160, 96, 64), (128, 96, 312)]
     rigs = [_rig(k, shapes, seed0=700) for k in range(len(shapes))]
     srv = sg.Server(0, 4 << 30)
