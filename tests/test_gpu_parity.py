@@ -140,6 +140,23 @@ def test_max_disparity_512(ctx, port):
     assert np.array_equal(got, want)
 
 
+def test_max_disparity_512_band_heights(gpu_lib, port):
+    """dc = 512 with bands of 9 rows (cost copies of 4 pixels) and of 11 and 12 rows (copies of 2 pixels, the
+    aggregation's second instantiation at this d-stride) vs the oracle."""
+    rng = np.random.default_rng(1512)
+    views = [rng.integers(0, 256, (12, 20), dtype=np.uint8) for _ in range(5)]
+    want = port.compute(views, 512, modes=(True, False, False))[0]
+    for rows in (9, 11, 12):
+        c = sg.Context(0)
+        c.tune_set(sg.TUNE_SGM_ROWS, rows)
+        c.load_views(views)
+        c.set_max_disparity(512)
+        got = c.compute(True, False, False)[0]
+        assert c.plan()["rows"] == rows
+        assert np.array_equal(got, want), "%d-row bands: %d px differ" % (rows, int((got != want).sum()))
+        c.close()
+
+
 def test_bgr_input_matches_gray(ctx):
     views, _ = synth.make_rig(96, 64, 2, 16, seed=9, tiles=3)
     ctx.load_views(views)
