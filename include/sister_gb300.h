@@ -120,8 +120,10 @@ enum {
                                   row-recursive 3x3 medians that follow the WTA rows */
     SISTER_STAGE_MASKS = 5,    /* LR check and confidence masks */
     SISTER_STAGE_COST = 6,     /* masked multiview cost volume (once per computed mode) */
-    SISTER_STAGE_AGGREGATE = 7, /* 8-path aggregation, both passes concurrently (once per computed mode) */
-    SISTER_STAGE_WTA = 8        /* sum of the two passes + winner-take-all, crop, *255 (once per mode) */
+    SISTER_STAGE_AGGREGATE = 7, /* 8-path aggregation, both passes concurrently, and the final winner-take-all,
+                                   crop and *255 of every output row in the same launch (all computed modes) */
+    SISTER_STAGE_WTA = 8        /* the final winner-take-all as its own kernel: only with SISTER_TUNE_FULL_DISP
+                                   (the padded map); otherwise ~0 */
 };
 /* Enable/disable event recording for subsequent computes (no reference counterpart: the reference only
  * prints clock() around whole modes, SisterMultiviewDisparities.hpp:73-89). */
